@@ -1,0 +1,150 @@
+/*
+ * nebc7_gb300 -- BC7 block encoder for NVIDIA GB300 (sm_103a), C ABI.
+ *
+ * Drop-in for the block compressor of andrewevstyukhin/nebc7: every 128-bit
+ * block it writes is bit-identical to the reference CPU encoder's for the
+ * same input, mask, starting blocks, preset and flags.
+ *
+ * Two layers:
+ *
+ *  1. The reference's own interfaces, as plain C:
+ *       nebc7_GetBc7Core      fills an IBc7Core vtable
+ *                             (reference src/Bc7Core.h:316-322, src/Bc7Core.cpp:1998);
+ *       nebc7_ProcessTexture  whole-texture job entry
+ *                             (reference src/Worker.h:6, src/Worker.cpp:249).
+ *     The reference passes its error accumulators by C++ reference; here they
+ *     are pointers (the same machine-level ABI).  The reference fixes
+ *     kDenoise / kDenoiseStep at compile time (src/Bc7Mode.h:10-13); here
+ *     nebc7_set_preset selects them at run time.
+ *
+ *  2. Direct entries on device or host buffers (nebc7_encode_*,
+ *     nebc7_decode_*), with explicit settings and CUDA streams.
+ *
+ * All functions return 0 on success or one of the NEBC7_E* codes.  The
+ * IBc7Core kernels have no error channel (the reference's are noexcept);
+ * they leave their outputs untouched on failure and record the code for
+ * nebc7_last_error().
+ */
+#ifndef NEBC7_GB300_H
+#define NEBC7_GB300_H
+
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum
+{
+	NEBC7_OK = 0,
+	NEBC7_EINVAL = 1,        /* bad argument (sizes, alignment, preset) */
+	NEBC7_ECUDA = 2,         /* a CUDA call failed */
+	NEBC7_ENOMEM = 3,        /* device memory could not be allocated */
+	NEBC7_EUNSUPPORTED = 4,  /* requested pass not available in this build */
+	NEBC7_ELIMIT = 5,        /* a device-side iteration limit was reached */
+	NEBC7_ETOOBIG = 6        /* request exceeds a fixed capacity */
+};
+
+/* ---- reference block API (src/Bc7Core.h:294-322) ---------------------- */
+
+typedef struct WorkerItem
+{
+	uint8_t* _Output;   /* 16 bytes: starting block in, encoded block out */
+	uint8_t* _Cell;     /* 4 rows of 4 BGRA pixels, `stride` bytes apart */
+	uint8_t* _Mask;     /* 4 rows of 4 masks (bytes A,G,R,B), same stride */
+} WorkerItem;
+
+typedef struct BlockSSIM
+{
+	double Alpha, Color;
+} BlockSSIM;
+
+typedef void (*PInitTables)(bool doDraft, bool doNormal, bool doSlow, bool linearData);
+typedef void (*PBlockKernel)(const WorkerItem* begin, const WorkerItem* end, int stride,
+	int64_t* pErrorAlpha, int64_t* pErrorColor, BlockSSIM* pssim);
+typedef int (*PGetWeight)(void);
+
+typedef struct IBc7Core
+{
+	PInitTables pInitTables;
+	PBlockKernel pDecompress, pCompress;
+	PGetWeight pGetWeightAlpha, pGetWeightColor;
+} IBc7Core;
+
+/* Replaces GetBc7Core (src/Bc7Core.cpp:1998): fills the vtable; false if no
+   usable CUDA device is present.  pInitTables (src/Bc7Core.cpp:1877) stores
+   the flags and weights and builds the level tables of the current preset
+   on the current device.  pCompress (src/Bc7Core.cpp:1936) encodes the items
+   on the GPU and *adds* Error.Alpha << 2kD, (Error.Total - Error.Alpha) <<
+   2kD and the SSIM values to the accumulators, as the reference does.
+   pDecompress (src/Bc7Core.cpp:1904) writes the decoded BGRA rows to _Cell. */
+bool nebc7_GetBc7Core(void* bc7Core);
+
+/* Replaces ProcessTexture (src/Worker.h:6): splits the padded texture
+   (src_w, src_h multiples of 4) into 4x4 blocks and runs `blockKernel`
+   (pCompress or pDecompress of this library) on all of them in one launch.
+   Host buffers; block_size must be 16.  Accumulators are assigned, like the
+   reference's Worker::Run. */
+void nebc7_ProcessTexture(uint8_t* dst, uint8_t* src_bgra, uint8_t* mask_agrb, int stride, int src_w, int src_h,
+	PBlockKernel blockKernel, size_t block_size, int64_t* pErrorAlpha, int64_t* pErrorColor, BlockSSIM* pssim);
+
+/* The compile-time preset of the reference (src/Bc7Mode.h:10-13) chosen at
+   run time: denoise (kDenoise) 0 or 1, denoiseStep (kDenoiseStep) >= 0.
+   Default 1, 9.  Takes effect for later calls. */
+int nebc7_set_preset(int denoise, int denoiseStep);
+
+/* Last error recorded by a call without an error channel. */
+int nebc7_last_error(void);
+
+/* ---- direct entries ----------------------------------------------------- */
+
+typedef struct nebc7_settings
+{
+	int denoise;        /* kDenoise: 0 or 1 */
+	int denoiseStep;    /* kDenoiseStep */
+	int doDraft;        /* bounding-box passes (the CLI always sets this) */
+	int doNormal;       /* refinement + full searches of modes 2, 0 / 5, 4, 7 */
+	int doSlow;         /* full searches of every mode */
+	int linearData;     /* /data: equal channel weights */
+} nebc7_settings;
+
+/* Encodes a padded texture (w, h multiples of 4) on the GPU.  Device
+   pointers: d_dst holds w*h/16 blocks (16-byte aligned), read as the starting
+   blocks (all-zero bytes = start from scratch) and overwritten; d_bgra / d_mask
+   hold rows of w pixels `stride` bytes apart (4-byte aligned); d_mask may be
+   null for a full mask.  `stream` is a cudaStream_t (null = default).
+   If errs / ssim are non-null the call waits for the stream and stores the
+   error sums (alpha, color) and SSIM sums there; otherwise it only enqueues. */
+int nebc7_encode_device(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w, int h,
+	const nebc7_settings* settings, int64_t* errs, double* ssim, void* stream);
+
+/* Same with host buffers: copies in, encodes, copies the blocks back. */
+int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int w, int h,
+	const nebc7_settings* settings, int64_t* errs, double* ssim);
+
+/* Independent blocks: cells / masks hold 64 bytes per block (4 rows of 4
+   pixels), io 16 bytes per block (starting block in, result out).  Host
+   buffers. */
+int nebc7_encode_blocks_host(const uint8_t* cells, const uint8_t* masks, uint8_t* io, int n,
+	const nebc7_settings* settings, int64_t* errs, double* ssim);
+
+/* Decodes blocks to BGRA (device pointers; rows of w pixels, `stride`
+   bytes apart). */
+int nebc7_decode_device(const uint8_t* d_blocks, uint8_t* d_bgra, long long stride, int w, int h, void* stream);
+
+/* Decodes n blocks to 64 bytes of BGRA each (host buffers). */
+int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
+
+/* Builds the level tables of `denoise` on the current device ahead of use. */
+int nebc7_init_device(int denoise);
+
+/* Persistent-grid sizing of the encode kernel: CTAs per SM and warps per CTA. */
+int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NEBC7_GB300_H */

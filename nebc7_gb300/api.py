@@ -1,0 +1,243 @@
+"""Python host side of the encoder, shaped like the reference's interfaces.
+
+* ``Bc7Core`` mirrors the reference's ``IBc7Core`` vtable (reference
+  src/Bc7Core.h:316-322): ``init_tables`` (pInitTables), ``compress`` /
+  ``decompress`` (pCompress / pDecompress over independent 4x4 cells) and
+  ``weight_alpha`` / ``weight_color``.  The preset (kDenoise, kDenoiseStep),
+  a compile-time constant in the reference (src/Bc7Mode.h:10-13), is a
+  constructor argument here.
+* ``process_texture`` mirrors ``ProcessTexture`` (src/Worker.h:6) on a padded
+  texture.
+* ``encode_image`` mirrors the CLI driver (src/Bc7Compress.cpp:267): CLI
+  flags, padding to multiples of 4, the alpha outline mask, the encode, and
+  the qMSE / qPSNR / wSSIM report.
+* ``encode_device`` works on resident device buffers (torch CUDA tensors or raw
+  pointers) with a CUDA stream.
+
+Everything runs on the GPU through the C ABI; nothing here computes blocks.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native
+from ._native import NativeError, Settings, check
+
+
+@dataclass(frozen=True)
+class Preset:
+    """The reference's kDenoise / kDenoiseStep pair (src/Bc7Mode.h:10-13)."""
+
+    denoise: int = 1
+    step: int = 9
+
+
+DEFAULT = Preset(1, 9)
+PRECISE = Preset(0, 0)
+
+
+def _settings(preset: Preset, draft: bool, normal: bool, slow: bool, linear: bool) -> Settings:
+    return Settings(int(preset.denoise), int(preset.step), int(draft), int(normal), int(slow), int(linear))
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+@dataclass
+class EncodeStats:
+    """Error and SSIM sums as the reference's block kernel accumulates them
+    (src/Bc7Core.cpp:1980-1984)."""
+
+    err_alpha: int
+    err_color: int
+    ssim_alpha: float
+    ssim_color: float
+
+
+class Bc7Core:
+    """The IBc7Core block API over the GPU encoder."""
+
+    def __init__(self, preset: Preset = DEFAULT):
+        self.preset = preset
+        self._lib = _native.load()
+        self._flags = (True, True, False, False)
+
+    def init_tables(self, do_draft: bool = True, do_normal: bool = True, do_slow: bool = False,
+                    linear_data: bool = False) -> None:
+        """pInitTables (src/Bc7Core.cpp:1877): flags, weights and resident tables."""
+        self._flags = (bool(do_draft), bool(do_normal), bool(do_slow), bool(linear_data))
+        check(self._lib.nebc7_init_device(int(self.preset.denoise)), "init tables")
+
+    def weight_alpha(self) -> int:
+        return 1 if self._flags[3] else 1000
+
+    def weight_color(self) -> int:
+        return 3 if self._flags[3] else 715 + 213 + 72
+
+    def settings(self) -> Settings:
+        return _settings(self.preset, *self._flags)
+
+    def compress(self, cells: np.ndarray, masks: np.ndarray, blocks: np.ndarray) -> EncodeStats:
+        """pCompress over n cells: cells / masks uint8[n, 64], blocks uint8[n, 16]
+        (starting blocks in, results out)."""
+        cells = np.ascontiguousarray(cells, dtype=np.uint8)
+        masks = np.ascontiguousarray(masks, dtype=np.uint8)
+        if blocks.dtype != np.uint8 or not blocks.flags.c_contiguous:
+            raise ValueError("blocks must be a C-contiguous uint8 array")
+        n = blocks.shape[0]
+        if cells.shape != (n, 64) or masks.shape != (n, 64) or blocks.shape != (n, 16):
+            raise ValueError("expected cells/masks [n, 64] and blocks [n, 16]")
+        err = np.zeros(2, np.int64)
+        ssim = np.zeros(2, np.float64)
+        s = self.settings()
+        check(self._lib.nebc7_encode_blocks_host(_ptr(cells), _ptr(masks), _ptr(blocks), n, ctypes.byref(s),
+                                                 _ptr(err), _ptr(ssim)), "compress")
+        return EncodeStats(int(err[0]), int(err[1]), float(ssim[0]), float(ssim[1]))
+
+    def decompress(self, blocks: np.ndarray) -> np.ndarray:
+        """pDecompress: uint8[n, 16] blocks -> uint8[n, 64] BGRA cells."""
+        blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+        out = np.zeros((blocks.shape[0], 64), np.uint8)
+        check(self._lib.nebc7_decode_blocks_host(_ptr(blocks), _ptr(out), blocks.shape[0]), "decompress")
+        return out
+
+    def process_texture(self, dst: np.ndarray, src_bgra: np.ndarray, mask_agrb: np.ndarray | None,
+                        width: int, height: int, stride: int | None = None) -> EncodeStats:
+        """ProcessTexture (src/Worker.h:6) with the compress kernel on a padded
+        texture held in host arrays."""
+        stride = width * 4 if stride is None else stride
+        src_bgra = np.ascontiguousarray(src_bgra, dtype=np.uint8)
+        mp = None
+        if mask_agrb is not None:
+            mask_agrb = np.ascontiguousarray(mask_agrb, dtype=np.uint8)
+            mp = _ptr(mask_agrb)
+        err = np.zeros(2, np.int64)
+        ssim = np.zeros(2, np.float64)
+        s = self.settings()
+        check(self._lib.nebc7_encode_host(_ptr(dst), _ptr(src_bgra), mp, stride, width, height, ctypes.byref(s),
+                                          _ptr(err), _ptr(ssim)), "process_texture")
+        return EncodeStats(int(err[0]), int(err[1]), float(ssim[0]), float(ssim[1]))
+
+
+def padded_size(w: int, h: int) -> tuple[int, int]:
+    """src/Bc7Compress.cpp:397-398: at least 4, rounded up to a multiple of 4."""
+    return (max(4, w) + 3) & ~3, (max(4, h) + 3) & ~3
+
+
+def pad_texture(img_bgra: np.ndarray) -> np.ndarray:
+    """Edge replication to the padded size (src/Bc7Compress.cpp:411-426)."""
+    h, w = img_bgra.shape[:2]
+    pw, ph = padded_size(w, h)
+    out = np.empty((ph, pw, 4), np.uint8)
+    out[:h, :w] = img_bgra
+    out[:h, w:] = img_bgra[:, w - 1:w]
+    out[h:] = out[h - 1:h]
+    return out
+
+
+def outline_mask(padded_bgra: np.ndarray, radius: int) -> np.ndarray:
+    """Alpha mask with an outline (src/Bc7Compress.cpp:33-105): colour is
+    visible where any pixel of the (2r+1)^2 neighbourhood has non-zero alpha;
+    alpha is always visible.  Bytes A,G,R,B per pixel."""
+    h, w = padded_bgra.shape[:2]
+    on = (padded_bgra[:, :, 3] != 0).astype(np.int32)
+    pad = np.pad(on, radius)
+    c = pad.cumsum(0).cumsum(1)
+    c = np.pad(c, ((1, 0), (1, 0)))
+    k = 2 * radius + 1
+    box = c[k:k + h, k:k + w] - c[0:h, k:k + w] - c[k:k + h, 0:w] + c[0:h, 0:w]
+    mask = np.empty((h, w, 4), np.uint8)
+    mask[:, :, 0] = 0xFF
+    v = np.where(box > 0, 0xFF, 0).astype(np.uint8)
+    mask[:, :, 1] = v
+    mask[:, :, 2] = v
+    mask[:, :, 3] = v
+    return mask
+
+
+def parse_flags(flags: str) -> dict:
+    """CLI switches (src/Bc7Compress.cpp:269-363) that affect the encode."""
+    o = dict(draft=True, normal=True, slow=False, mask=True, radius=1, linear=False)
+    for f in flags.split():
+        if f == "/draft":
+            o.update(draft=True, normal=False, slow=False)
+        elif f == "/slow":
+            o.update(draft=True, normal=True, slow=True)
+        elif f == "/nomask":
+            o["mask"] = False
+        elif f == "/retina":
+            o["radius"] = 2
+        elif f == "/data":
+            o.update(mask=False, linear=True)
+        elif f == "/compare":
+            o.update(draft=False, normal=False, slow=False)
+        elif f == "/noflip":
+            pass
+        else:
+            raise ValueError(f"unsupported flag {f!r}")
+    return o
+
+
+@dataclass
+class EncodedImage:
+    blocks: np.ndarray       # uint8[padded_h // 4 * padded_w // 4, 16]
+    width: int               # padded texture size
+    height: int
+    stats: EncodeStats
+
+    def report(self, weight_alpha: int, weight_color: int) -> dict:
+        """qMSE / qPSNR / SSIM as the CLI prints them (src/Bc7Compress.cpp:490-518)."""
+        px = self.width * self.height
+        out = {}
+        if self.stats.err_alpha > 0:
+            out["A"] = dict(qMSE=self.stats.err_alpha / weight_alpha / px,
+                            qPSNR=10.0 * math.log(255.0 * 255.0 * weight_alpha * px / self.stats.err_alpha) / math.log(10.0),
+                            SSIM_4x4=self.stats.ssim_alpha * 16.0 / px)
+        if self.stats.err_color > 0:
+            out["RGB"] = dict(qMSE=self.stats.err_color / weight_color / px,
+                              qPSNR=10.0 * math.log(255.0 * 255.0 * weight_color * px / self.stats.err_color) / math.log(10.0),
+                              wSSIM_4x4=self.stats.ssim_color * 16.0 / px)
+        return out
+
+
+def encode_image(img_bgra: np.ndarray, flags: str = "", preset: Preset = DEFAULT,
+                 start: np.ndarray | None = None) -> EncodedImage:
+    """The CLI's encode path on an in-memory BGRA image (top-down rows)."""
+    o = parse_flags(flags)
+    padded = pad_texture(np.ascontiguousarray(img_bgra, dtype=np.uint8))
+    ph, pw = padded.shape[:2]
+    mask = outline_mask(padded, o["radius"]) if o["mask"] else None
+    core = Bc7Core(preset)
+    core.init_tables(o["draft"], o["normal"], o["slow"], o["linear"])
+    blocks = np.zeros(((ph // 4) * (pw // 4), 16), np.uint8) if start is None else np.array(start, np.uint8)
+    stats = core.process_texture(blocks, padded, mask, pw, ph)
+    return EncodedImage(blocks, pw, ph, stats)
+
+
+def encode_device(dst_ptr: int, bgra_ptr: int, mask_ptr: int | None, stride: int, width: int, height: int,
+                  preset: Preset = DEFAULT, draft: bool = True, normal: bool = True, slow: bool = False,
+                  linear: bool = False, stream: int = 0, want_stats: bool = False) -> EncodeStats | None:
+    """Encodes device-resident buffers (raw CUDA pointers) on `stream`."""
+    lib = _native.load()
+    s = _settings(preset, draft, normal, slow, linear)
+    if want_stats:
+        err = np.zeros(2, np.int64)
+        ssim = np.zeros(2, np.float64)
+        check(lib.nebc7_encode_device(dst_ptr, bgra_ptr, mask_ptr, stride, width, height, ctypes.byref(s),
+                                      _ptr(err), _ptr(ssim), stream), "encode_device")
+        return EncodeStats(int(err[0]), int(err[1]), float(ssim[0]), float(ssim[1]))
+    check(lib.nebc7_encode_device(dst_ptr, bgra_ptr, mask_ptr, stride, width, height, ctypes.byref(s),
+                                  None, None, stream), "encode_device")
+    return None
+
+
+__all__ = [
+    "Bc7Core", "Preset", "DEFAULT", "PRECISE", "EncodeStats", "EncodedImage", "NativeError",
+    "encode_image", "encode_device", "pad_texture", "outline_mask", "padded_size", "parse_flags",
+]

@@ -1,0 +1,290 @@
+/*
+ * BC7 block encoder for sm_103a -- the per-block scheduler and the encode /
+ * decode kernels.
+ *
+ * KEncode is a persistent kernel: each warp takes the next block index from
+ * a global counter and runs the reference's per-block pipeline
+ * (src/Bc7Core.cpp:1516-1823 CompressBlock) on it: decode the block already
+ * in `dst` (incremental re-encode), measure it, and unless it is exact run
+ * the mode chain with error stepping, pack the winner and self-check it.
+ * Block costs differ by orders of magnitude (an exact block stops at once, a
+ * hard one searches every partition), so blocks are dealt one at a time.
+ */
+#pragma once
+
+#include "bc7_fast.cuh"
+#include "bc7_search.cuh"
+
+namespace nebc7 {
+
+struct BlockResult
+{
+	int errAlpha;     /* Error.Alpha << 2 kDenoise */
+	int errColor;     /* (Error.Total - Error.Alpha) << 2 kDenoise */
+	double ssimAlpha, ssimColor;
+};
+
+/* Per-launch description of where the blocks are. */
+struct Job
+{
+	uint8_t* dst;            /* 16 bytes per block, read as the starting block */
+	const uint8_t* bgra;     /* top-left pixel of block 0 */
+	const uint8_t* mask;     /* same layout, A,G,R,B bytes; null = all 0xFF */
+	long long stride;        /* bytes between pixel rows */
+	int blocksW;             /* blocks per block row */
+	int nblocks;
+	BlockResult* results;    /* optional, one per block */
+	int* counter;            /* work queue head, zero before launch */
+	int* status;             /* set non-zero on an internal limit */
+};
+
+constexpr int kWarpsPerCta = 4;
+
+template<int kD>
+__device__ void EncodeBlock(WarpState& st, const Job& job, const LevelTables& T, const Params& P, int k, int lane)
+{
+	const int bx = k % job.blocksW, by = k / job.blocksW;
+	const long long base = (long long)by * 4 * job.stride + (long long)bx * 16;
+
+	/* coalesced load: lanes 0..15 read one BGRA pixel, 16..31 its mask */
+	{
+		const int i = lane & 15;
+		const long long off = base + (long long)(i >> 2) * job.stride + (i & 3) * 4;
+		if (lane < 16)
+		{
+			const uchar4 p = *reinterpret_cast<const uchar4*>(job.bgra + off);
+			st.img[i][0] = p.w;
+			st.img[i][1] = p.y;
+			st.img[i][2] = p.z;
+			st.img[i][3] = p.x;
+		}
+		else
+		{
+			uchar4 m = make_uchar4(0xFF, 0xFF, 0xFF, 0xFF);
+			if (job.mask)
+				m = *reinterpret_cast<const uchar4*>(job.mask + off);
+			st.msk[i][0] = m.x;
+			st.msk[i][1] = m.y;
+			st.msk[i][2] = m.z;
+			st.msk[i][3] = m.w;
+		}
+	}
+	const uint4 blk = *reinterpret_cast<const uint4*>(job.dst + (long long)k * 16);
+	__syncwarp();
+
+	uint64_t lo = uint64_t(blk.x) | (uint64_t(blk.y) << 32);
+	uint64_t hi = uint64_t(blk.z) | (uint64_t(blk.w) << 32);
+	if (!(lo & 0xFF))
+	{
+		/* src/Bc7Core.cpp:1518-1522: an empty block starts as a zero mode 6 block */
+		lo = 1u << 6;
+		hi = 0;
+	}
+	const uint64_t savedLo = lo, savedHi = hi;
+
+	/* widened masks and masked data (src/Bc7Core.cpp:52-86) */
+	uint32_t visBit = 0;
+	unsigned alphaAnd = 0xFF;
+	if (lane < 16)
+	{
+		for (int c = 0; c < 4; c++)
+		{
+			const uint16_t m = uint16_t(int16_t(int8_t(st.msk[lane][c])));
+			st.mk[lane][c] = m;
+			st.px[lane][c] = uint16_t(st.img[lane][c] & m);
+		}
+		visBit = (st.mk[lane][1] >> lane) & 1;
+		alphaAnd = st.px[lane][0];
+	}
+	CellRegs R;
+	R.visible = __ballot_sync(kFull, visBit != 0) & 0xFFFF;
+	R.opaque = __reduce_and_sync(kFull, alphaAnd) == 255;
+
+	DecodeToState(st, lo, hi, R.best, R.bestParam, R.bestMode, lane);
+	CompareBlocks<kD>(st, P, lane, R.errAlpha, R.errTotal);
+
+	double qa = 1.0, qc = 1.0;
+	if (R.errTotal > 0)
+	{
+		R.a1 = AreaStats(st, R, P, 0xFFFF);
+		R.a1.zero = 0;
+		BuildAreaList(st.area1, st, R, 0xFFFF, 0, lane);
+		R.personalMode = -1;
+		R.personalParam = -1;
+
+		if (P.doDraft)
+		{
+			const int step = R.a1.active * ((P.denoiseStep * (R.a1.opaque ? P.wColor : P.wColorAlpha)) >> (kD + kD));
+			R.denoiseStep = step;
+			/* src/Bc7Core.cpp:24-50 */
+			{
+				int e = 0;
+				if (!R.a1.opaque && lane < 16)
+				{
+					int da = int(st.area1.px[lane][0]) ^ 255;
+					da = kD ? (da >> kD) : (da > 0x7F ? 0x7F : da);
+					e = da * da;
+				}
+				e = int(__reduce_add_sync(kFull, unsigned(e)));
+				R.opaqueAlphaError = R.a1.opaque ? 0 : e * P.wA;
+			}
+			const int water = R.errTotal;
+
+			if (R.errTotal > step)
+			{
+				if (kD > 0 || P.denoiseStep > 0)
+					FastMode6<kD, true>(st, R, P, T);
+				if (R.errTotal > step)
+				{
+					FastMode6<kD, false>(st, R, P, T);
+					if (R.errTotal > step)
+					{
+						FastRot<kD, 4>(st, R, P, lane);
+						if (R.errTotal > step)
+						{
+							FastRot<kD, 5>(st, R, P, lane);
+							if (R.errTotal > step)
+								FastMode7<kD>(st, R, P, T, lane);
+						}
+					}
+				}
+			}
+
+			if (int(int16_t(R.a1.minmax[0])) > 255 - 16)
+			{
+				const int gate = R.opaqueAlphaError + step;
+				if (R.errTotal > gate)
+				{
+					FastOpaque<kD, 3>(st, R, P, lane);
+					if (R.errTotal > gate)
+					{
+						FastOpaque<kD, 1>(st, R, P, lane);
+						if (R.errTotal > gate)
+						{
+							FastOpaque<kD, 2>(st, R, P, lane);
+							if (R.errTotal > gate)
+								FastOpaque<kD, 0>(st, R, P, lane);
+						}
+					}
+				}
+			}
+
+			if (P.doNormal)
+				NormalPasses<kD>(st, R, P, T, job.status, lane);
+
+			if (water > R.errTotal)
+				FinalPack<kD>(st, R, P, lo, hi, lane);
+		}
+
+		/* self-check (src/Bc7Core.cpp:1799-1807): the packed block must decode to
+		   the tracked error, otherwise the starting block is kept */
+		Ep dummy[3];
+		int dp, dm;
+		DecodeToState(st, lo, hi, dummy, dp, dm, lane);
+		int ea, et;
+		CompareBlocks<kD>(st, P, lane, ea, et);
+		if (ea != R.errAlpha || et != R.errTotal)
+		{
+			lo = savedLo;
+			hi = savedHi;
+		}
+		CompareBlocksSSIM(st, P, lane, qa, qc);
+	}
+
+	if (lane == 0)
+	{
+		*reinterpret_cast<uint4*>(job.dst + (long long)k * 16) =
+			make_uint4(unsigned(lo), unsigned(lo >> 32), unsigned(hi), unsigned(hi >> 32));
+		if (job.results)
+		{
+			BlockResult r;
+			r.errAlpha = int(unsigned(R.errAlpha) << (kD + kD));
+			r.errColor = int(unsigned(R.errTotal - R.errAlpha) << (kD + kD));
+			r.ssimAlpha = qa;
+			r.ssimColor = qc;
+			job.results[k] = r;
+		}
+	}
+	__syncwarp();
+}
+
+template<int kD>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) KEncode(Job job, LevelTables T, Params P)
+{
+	__shared__ WarpState states[kWarpsPerCta];
+	const int lane = threadIdx.x & 31;
+	WarpState& st = states[threadIdx.x >> 5];
+	for (;;)
+	{
+		int k = 0;
+		if (lane == 0)
+			k = atomicAdd(job.counter, 1);
+		k = __shfl_sync(kFull, k, 0);
+		if (k >= job.nblocks)
+			break;
+		EncodeBlock<kD>(st, job, T, P, k, lane);
+	}
+}
+
+/* Decodes blocks to BGRA pixels (src/Bc7Core.cpp:1904 DecompressKernel):
+   one thread per pixel. */
+__global__ void KDecode(const uint8_t* blocks, uint8_t* bgra, long long stride, int blocksW, int nblocks)
+{
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long long)nblocks * 16)
+		return;
+	const int k = int(t >> 4), i = int(t & 15);
+	const uint4 b = *reinterpret_cast<const uint4*>(blocks + (long long)k * 16);
+	const uint64_t lo = uint64_t(b.x) | (uint64_t(b.y) << 32);
+	const uint64_t hi = uint64_t(b.z) | (uint64_t(b.w) << 32);
+	uint8_t px[4];
+	Ep best[3];
+	int param, mode;
+	DecodeBlock(lo, hi, i, px, best, param, mode);
+	const int bx = k % blocksW, by = k / blocksW;
+	uint8_t* p = bgra + ((long long)by * 4 + (i >> 2)) * stride + (long long)bx * 16 + (i & 3) * 4;
+	*reinterpret_cast<uchar4*>(p) = make_uchar4(px[3], px[1], px[2], px[0]);
+}
+
+/* Deterministic reduction of the per-block results: a fixed-shape tree, so
+   repeated runs give identical double sums. */
+__global__ void KReduceResults(const BlockResult* r, int n, long long* errs, double* ssims)
+{
+	__shared__ long long sa[256], sc[256];
+	__shared__ double qa[256], qc[256];
+	const int t = threadIdx.x;
+	long long a = 0, c = 0;
+	double x = 0, y = 0;
+	for (int i = t; i < n; i += 256)
+	{
+		a += r[i].errAlpha;
+		c += r[i].errColor;
+		x = __dadd_rn(x, r[i].ssimAlpha);
+		y = __dadd_rn(y, r[i].ssimColor);
+	}
+	sa[t] = a;
+	sc[t] = c;
+	qa[t] = x;
+	qc[t] = y;
+	__syncthreads();
+	for (int s = 128; s > 0; s >>= 1)
+	{
+		if (t < s)
+		{
+			sa[t] += sa[t + s];
+			sc[t] += sc[t + s];
+			qa[t] = __dadd_rn(qa[t], qa[t + s]);
+			qc[t] = __dadd_rn(qc[t], qc[t + s]);
+		}
+		__syncthreads();
+	}
+	if (t == 0)
+	{
+		errs[0] = sa[0];
+		errs[1] = sc[0];
+		ssims[0] = qa[0];
+		ssims[1] = qc[0];
+	}
+}
+
+} // namespace nebc7

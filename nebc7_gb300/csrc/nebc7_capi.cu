@@ -1,0 +1,539 @@
+/*
+ * nebc7_gb300 -- host side of the C ABI declared in include/nebc7_gb300.h.
+ *
+ * Owns the per-device resident level tables (built on the device the first
+ * time a preset's kDenoise is used), launches the persistent encode kernel
+ * with stream-ordered scratch (work counter, per-block results), and adapts
+ * the reference's IBc7Core / ProcessTexture interfaces onto it.
+ */
+#include "bc7_tables.cuh"
+#include "bc7_encode.cuh"
+
+#include "../../include/nebc7_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string.h>
+#include <vector>
+
+using namespace nebc7;
+
+namespace {
+
+constexpr int kMaxDevices = 16;
+
+struct DeviceTables
+{
+	bool built = false;
+	LevelTables t{};
+	void* mem[14] = {};
+};
+
+std::mutex gMutex;
+DeviceTables gTables[kMaxDevices][2];
+int gLastError = NEBC7_OK;
+
+/* InitTables state of the IBc7Core adapter (src/Bc7Core.cpp:20-22, 1877) */
+nebc7_settings gCore = { 1, 9, 1, 1, 0, 0 };
+
+int SetError(int e)
+{
+	gLastError = e;
+	return e;
+}
+
+#define CK(x)                                \
+	do                                       \
+	{                                        \
+		if ((x) != cudaSuccess)              \
+			return SetError(NEBC7_ECUDA);    \
+	} while (0)
+
+int BuildTables(int dev, int denoise, const LevelTables** out)
+{
+	std::lock_guard<std::mutex> lock(gMutex);
+	if (dev < 0 || dev >= kMaxDevices)
+		return SetError(NEBC7_EINVAL);
+	DeviceTables& D = gTables[dev][denoise];
+	if (!D.built)
+	{
+		const size_t sizes[14] = {
+			size_t(256) * 65536, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
+			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
+			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
+			size_t(256) * 128 * 2, size_t(256) * 32 * 2,
+			size_t(256) * 32768, size_t(256) * 32768,
+		};
+		for (int i = 0; i < 14; i++)
+		{
+			if (cudaMalloc(&D.mem[i], sizes[i]) != cudaSuccess)
+			{
+				for (int j = 0; j < i; j++)
+					cudaFree(D.mem[j]);
+				return SetError(NEBC7_ENOMEM);
+			}
+		}
+		uint8_t* d3v8 = nullptr;
+		if (cudaMalloc(&d3v8, size_t(256) * 65536) != cudaSuccess)
+			return SetError(NEBC7_ENOMEM);
+		uint8_t* d2v8 = (uint8_t*)D.mem[0];
+		const int tb = 256;
+		auto grid = [&](uint64_t n) { return unsigned((n + tb - 1) / tb); };
+		/* 3-bit index tables (reference src/Bc7Tables.cpp:587-641) */
+		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d3v8, 8, denoise, 0);
+		KReduce<<<grid(uint64_t(256) * 16384), tb>>>(d3v8, (uint8_t*)D.mem[7], 7, 1);
+		KReduce<<<grid(uint64_t(256) * 4096), tb>>>(d3v8, (uint8_t*)D.mem[8], 6, 0);
+		KReduce<<<grid(uint64_t(256) * 1024), tb>>>(d3v8, (uint8_t*)D.mem[9], 5, 0);
+		KCut<<<grid(256 * 128), tb>>>((uint8_t*)D.mem[7], (uint16_t*)D.mem[10], 7);
+		KCut<<<grid(256 * 32), tb>>>((uint8_t*)D.mem[9], (uint16_t*)D.mem[11], 5);
+		/* 2-bit index tables (:643-692) */
+		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d2v8, 4, denoise, 0);
+		KReduce<<<grid(uint64_t(256) * 16384), tb>>>(d2v8, (uint8_t*)D.mem[1], 7, 0);
+		KReduce<<<grid(uint64_t(256) * 4096), tb>>>(d2v8, (uint8_t*)D.mem[2], 6, 0);
+		KReduce<<<grid(uint64_t(256) * 1024), tb>>>(d2v8, (uint8_t*)D.mem[3], 5, 0);
+		KCut<<<grid(256 * 256), tb>>>(d2v8, (uint16_t*)D.mem[4], 8);
+		KCut<<<grid(256 * 64), tb>>>((uint8_t*)D.mem[2], (uint16_t*)D.mem[5], 6);
+		KCut<<<grid(256 * 32), tb>>>((uint8_t*)D.mem[3], (uint16_t*)D.mem[6], 5);
+		/* 4-bit and 2-of-4-bit nibble tables (:694-776) */
+		KBuildFull<<<grid(uint64_t(256) * 32768), tb>>>((uint8_t*)D.mem[12], 16, denoise, 1);
+		KHalfFrom2<<<grid(uint64_t(256) * 32768), tb>>>(d2v8, (uint8_t*)D.mem[13]);
+		const cudaError_t e = cudaDeviceSynchronize();
+		cudaFree(d3v8);
+		if (e != cudaSuccess)
+			return SetError(NEBC7_ECUDA);
+		LevelTables& t = D.t;
+		t.d2v8 = (const uint8_t*)D.mem[0];
+		t.d2v7 = (const uint8_t*)D.mem[1];
+		t.d2v6 = (const uint8_t*)D.mem[2];
+		t.d2v5 = (const uint8_t*)D.mem[3];
+		t.c2v8 = (const uint16_t*)D.mem[4];
+		t.c2v6 = (const uint16_t*)D.mem[5];
+		t.c2v5 = (const uint16_t*)D.mem[6];
+		t.d3v7s = (const uint8_t*)D.mem[7];
+		t.d3v6 = (const uint8_t*)D.mem[8];
+		t.d3v5 = (const uint8_t*)D.mem[9];
+		t.c3v7s = (const uint16_t*)D.mem[10];
+		t.c3v5 = (const uint16_t*)D.mem[11];
+		t.d4h = (const uint8_t*)D.mem[12];
+		t.d2h = (const uint8_t*)D.mem[13];
+		D.built = true;
+	}
+	*out = &D.t;
+	return NEBC7_OK;
+}
+
+Params MakeParams(const nebc7_settings& s)
+{
+	Params p;
+	p.denoiseStep = s.denoiseStep;
+	if (s.linearData)
+	{
+		p.wA = p.wG = p.wR = p.wB = 1;
+	}
+	else
+	{
+		p.wA = 1000;
+		p.wG = 715;
+		p.wR = 213;
+		p.wB = 72;
+	}
+	p.wColor = p.wG + p.wR + p.wB;
+	p.wColorAlpha = p.wColor + p.wA;
+	p.doDraft = s.doDraft;
+	p.doNormal = s.doNormal;
+	p.doSlow = s.doSlow;
+	return p;
+}
+
+int ValidateSettings(const nebc7_settings* s)
+{
+	if (!s || (s->denoise != 0 && s->denoise != 1) || s->denoiseStep < 0 || s->denoiseStep > 4096)
+		return NEBC7_EINVAL;
+	if ((s->doNormal || s->doSlow) && !kHasNormalPasses)
+		return NEBC7_EUNSUPPORTED;
+	return NEBC7_OK;
+}
+
+int GridFor(int nblocks)
+{
+	static int sms = 0;
+	if (!sms)
+	{
+		int dev = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+		if (sms <= 0)
+			sms = 1;
+	}
+	int perSm = 0;
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KEncode<1>, kWarpsPerCta * 32, 0);
+	if (perSm <= 0)
+		perSm = 1;
+	const int ctasNeeded = (nblocks + kWarpsPerCta - 1) / kWarpsPerCta;
+	const int g = sms * perSm;
+	return ctasNeeded < g ? ctasNeeded : g;
+}
+
+/* Enqueues one encode over `nblocks` blocks described by job geometry. */
+int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int blocksW, int nblocks,
+	const nebc7_settings& s, int64_t* errs, double* ssim, cudaStream_t stream)
+{
+	if (nblocks <= 0)
+	{
+		if (errs)
+			errs[0] = errs[1] = 0;
+		if (ssim)
+			ssim[0] = ssim[1] = 0;
+		return NEBC7_OK;
+	}
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	const LevelTables* T = nullptr;
+	if (int e = BuildTables(dev, s.denoise, &T))
+		return e;
+
+	const bool wantSums = errs || ssim;
+	const size_t resBytes = wantSums ? size_t(nblocks) * sizeof(BlockResult) : 0;
+	const size_t scratchBytes = 256 + resBytes + 64;
+	uint8_t* scratch = nullptr;
+	if (cudaMallocAsync((void**)&scratch, scratchBytes, stream) != cudaSuccess)
+		return SetError(NEBC7_ENOMEM);
+	int* counter = (int*)scratch;
+	int* status = counter + 1;
+	long long* sums = (long long*)(scratch + 64);
+	double* ssums = (double*)(scratch + 128);
+	BlockResult* results = wantSums ? (BlockResult*)(scratch + 256) : nullptr;
+	CK(cudaMemsetAsync(scratch, 0, 256, stream));
+
+	Job job;
+	job.dst = dst;
+	job.bgra = bgra;
+	job.mask = mask;
+	job.stride = stride;
+	job.blocksW = blocksW;
+	job.nblocks = nblocks;
+	job.results = results;
+	job.counter = counter;
+	job.status = status;
+	const Params P = MakeParams(s);
+	const int grid = GridFor(nblocks);
+	if (s.denoise)
+		KEncode<1><<<grid, kWarpsPerCta * 32, 0, stream>>>(job, *T, P);
+	else
+		KEncode<0><<<grid, kWarpsPerCta * 32, 0, stream>>>(job, *T, P);
+	CK(cudaGetLastError());
+
+	int rc = NEBC7_OK;
+	if (wantSums)
+	{
+		KReduceResults<<<1, 256, 0, stream>>>(results, nblocks, sums, ssums);
+		long long hs[2];
+		double hq[2];
+		int hstatus = 0;
+		CK(cudaMemcpyAsync(hs, sums, sizeof(hs), cudaMemcpyDeviceToHost, stream));
+		CK(cudaMemcpyAsync(hq, ssums, sizeof(hq), cudaMemcpyDeviceToHost, stream));
+		CK(cudaMemcpyAsync(&hstatus, status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+		CK(cudaStreamSynchronize(stream));
+		if (errs)
+		{
+			errs[0] = hs[0];
+			errs[1] = hs[1];
+		}
+		if (ssim)
+		{
+			ssim[0] = hq[0];
+			ssim[1] = hq[1];
+		}
+		if (hstatus)
+			rc = SetError(NEBC7_ELIMIT);
+	}
+	CK(cudaFreeAsync(scratch, stream));
+	return rc;
+}
+
+/* ---- IBc7Core adapter ------------------------------------------------- */
+
+void CoreInitTables(bool doDraft, bool doNormal, bool doSlow, bool linearData)
+{
+	gCore.doDraft = doDraft;
+	gCore.doNormal = doNormal;
+	gCore.doSlow = doSlow;
+	gCore.linearData = linearData;
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess)
+	{
+		SetError(NEBC7_ECUDA);
+		return;
+	}
+	const LevelTables* T = nullptr;
+	BuildTables(dev, gCore.denoise, &T);
+}
+
+/* Gathers the items' cells and masks into contiguous 64-byte blocks, encodes
+   them in one launch and scatters the blocks back (src/Bc7Core.cpp:1936). */
+void CoreCompress(const WorkerItem* begin, const WorkerItem* end, int stride, int64_t* pErrorAlpha, int64_t* pErrorColor, BlockSSIM* pssim)
+{
+	const int n = int(end - begin);
+	if (n <= 0)
+		return;
+	std::vector<uint8_t> cells(size_t(n) * 64), masks(size_t(n) * 64), io(size_t(n) * 16);
+	for (int i = 0; i < n; i++)
+	{
+		for (int r = 0; r < 4; r++)
+		{
+			memcpy(&cells[size_t(i) * 64 + r * 16], begin[i]._Cell + size_t(r) * stride, 16);
+			memcpy(&masks[size_t(i) * 64 + r * 16], begin[i]._Mask + size_t(r) * stride, 16);
+		}
+		memcpy(&io[size_t(i) * 16], begin[i]._Output, 16);
+	}
+	int64_t e[2] = { 0, 0 };
+	double q[2] = { 0, 0 };
+	if (nebc7_encode_blocks_host(cells.data(), masks.data(), io.data(), n, &gCore, e, q) != NEBC7_OK)
+		return;
+	for (int i = 0; i < n; i++)
+		memcpy(begin[i]._Output, &io[size_t(i) * 16], 16);
+	*pErrorAlpha += e[0];
+	*pErrorColor += e[1];
+	pssim->Alpha += q[0];
+	pssim->Color += q[1];
+}
+
+void CoreDecompress(const WorkerItem* begin, const WorkerItem* end, int stride, int64_t* pErrorAlpha, int64_t* pErrorColor, BlockSSIM* pssim)
+{
+	(void)pErrorAlpha;
+	(void)pErrorColor;
+	(void)pssim;
+	const int n = int(end - begin);
+	if (n <= 0)
+		return;
+	std::vector<uint8_t> blocks(size_t(n) * 16), bgra(size_t(n) * 64);
+	for (int i = 0; i < n; i++)
+		memcpy(&blocks[size_t(i) * 16], begin[i]._Output, 16);
+	if (nebc7_decode_blocks_host(blocks.data(), bgra.data(), n) != NEBC7_OK)
+		return;
+	for (int i = 0; i < n; i++)
+		for (int r = 0; r < 4; r++)
+			memcpy(begin[i]._Cell + size_t(r) * stride, &bgra[size_t(i) * 64 + r * 16], 16);
+}
+
+int CoreWeightAlpha()
+{
+	return gCore.linearData ? 1 : 1000;
+}
+
+int CoreWeightColor()
+{
+	return gCore.linearData ? 3 : 715 + 213 + 72;
+}
+
+} // namespace
+
+extern "C" {
+
+bool nebc7_GetBc7Core(void* bc7Core)
+{
+	int count = 0;
+	if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0)
+		return false;
+	IBc7Core* p = reinterpret_cast<IBc7Core*>(bc7Core);
+	p->pInitTables = &CoreInitTables;
+	p->pDecompress = &CoreDecompress;
+	p->pCompress = &CoreCompress;
+	p->pGetWeightAlpha = &CoreWeightAlpha;
+	p->pGetWeightColor = &CoreWeightColor;
+	return true;
+}
+
+void nebc7_ProcessTexture(uint8_t* dst, uint8_t* src_bgra, uint8_t* mask_agrb, int stride, int src_w, int src_h,
+	PBlockKernel blockKernel, size_t block_size, int64_t* pErrorAlpha, int64_t* pErrorColor, BlockSSIM* pssim)
+{
+	if (block_size != 16)
+	{
+		SetError(NEBC7_EINVAL);
+		return;
+	}
+	if (blockKernel == &CoreCompress)
+	{
+		int64_t e[2] = { 0, 0 };
+		double q[2] = { 0, 0 };
+		if (nebc7_encode_host(dst, src_bgra, mask_agrb, stride, src_w, src_h, &gCore, e, q) != NEBC7_OK)
+			return;
+		*pErrorAlpha = e[0];
+		*pErrorColor = e[1];
+		pssim->Alpha = q[0];
+		pssim->Color = q[1];
+	}
+	else if (blockKernel == &CoreDecompress)
+	{
+		/* decode every block back into src_bgra (the reference's /debug pass) */
+		const int bw = src_w / 4, bh = src_h / 4;
+		std::vector<uint8_t> bgra(size_t(bw) * bh * 64);
+		if (nebc7_decode_blocks_host(dst, bgra.data(), bw * bh) != NEBC7_OK)
+			return;
+		for (int k = 0; k < bw * bh; k++)
+			for (int r = 0; r < 4; r++)
+				memcpy(src_bgra + size_t(k / bw * 4 + r) * stride + size_t(k % bw) * 16, &bgra[size_t(k) * 64 + r * 16], 16);
+	}
+	else
+	{
+		SetError(NEBC7_EINVAL);
+	}
+}
+
+int nebc7_set_preset(int denoise, int denoiseStep)
+{
+	if ((denoise != 0 && denoise != 1) || denoiseStep < 0 || denoiseStep > 4096)
+		return SetError(NEBC7_EINVAL);
+	gCore.denoise = denoise;
+	gCore.denoiseStep = denoiseStep;
+	return NEBC7_OK;
+}
+
+int nebc7_last_error(void)
+{
+	return gLastError;
+}
+
+int nebc7_encode_device(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w, int h,
+	const nebc7_settings* settings, int64_t* errs, double* ssim, void* stream)
+{
+	if (int e = ValidateSettings(settings))
+		return SetError(e);
+	if (w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4 || (stride & 3))
+		return SetError(NEBC7_EINVAL);
+	if (((uintptr_t)d_dst & 15) || ((uintptr_t)d_bgra & 3) || ((uintptr_t)d_mask & 3))
+		return SetError(NEBC7_EINVAL);
+	const long long nb = (long long)(w / 4) * (h / 4);
+	if (nb > 0x7FFFFFFF)
+		return SetError(NEBC7_ETOOBIG);
+	return LaunchEncode(d_dst, d_bgra, d_mask, stride, w / 4, int(nb), *settings, errs, ssim, (cudaStream_t)stream);
+}
+
+int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int w, int h,
+	const nebc7_settings* settings, int64_t* errs, double* ssim)
+{
+	if (int e = ValidateSettings(settings))
+		return SetError(e);
+	if (w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4)
+		return SetError(NEBC7_EINVAL);
+	const size_t nb = size_t(w / 4) * (h / 4);
+	const size_t img = size_t(w) * 4 * h;
+	uint8_t *dd = nullptr, *db = nullptr, *dm = nullptr;
+	if (cudaMalloc(&dd, nb * 16) != cudaSuccess || cudaMalloc(&db, img) != cudaSuccess || (mask && cudaMalloc(&dm, img) != cudaSuccess))
+	{
+		cudaFree(dd);
+		cudaFree(db);
+		cudaFree(dm);
+		return SetError(NEBC7_ENOMEM);
+	}
+	int rc = NEBC7_OK;
+	if (cudaMemcpy2D(db, size_t(w) * 4, bgra, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice) != cudaSuccess ||
+		(mask && cudaMemcpy2D(dm, size_t(w) * 4, mask, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice) != cudaSuccess) ||
+		cudaMemcpy(dd, dst, nb * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	int64_t e[2];
+	double q[2];
+	if (rc == NEBC7_OK)
+		rc = LaunchEncode(dd, db, dm, (long long)w * 4, w / 4, int(nb), *settings, e, q, nullptr);
+	if (rc == NEBC7_OK && cudaMemcpy(dst, dd, nb * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	if (rc == NEBC7_OK)
+	{
+		if (errs)
+		{
+			errs[0] = e[0];
+			errs[1] = e[1];
+		}
+		if (ssim)
+		{
+			ssim[0] = q[0];
+			ssim[1] = q[1];
+		}
+	}
+	cudaFree(dd);
+	cudaFree(db);
+	cudaFree(dm);
+	return rc;
+}
+
+int nebc7_encode_blocks_host(const uint8_t* cells, const uint8_t* masks, uint8_t* io, int n,
+	const nebc7_settings* settings, int64_t* errs, double* ssim)
+{
+	if (int e = ValidateSettings(settings))
+		return SetError(e);
+	if (n < 0)
+		return SetError(NEBC7_EINVAL);
+	if (n == 0)
+	{
+		if (errs)
+			errs[0] = errs[1] = 0;
+		if (ssim)
+			ssim[0] = ssim[1] = 0;
+		return NEBC7_OK;
+	}
+	/* a column of blocks: stride 16, one block per block row */
+	return nebc7_encode_host(io, cells, masks, 16, 4, 4 * n, settings, errs, ssim);
+}
+
+int nebc7_decode_device(const uint8_t* d_blocks, uint8_t* d_bgra, long long stride, int w, int h, void* stream)
+{
+	if (w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4 || (stride & 3) || ((uintptr_t)d_blocks & 15))
+		return SetError(NEBC7_EINVAL);
+	const long long nb = (long long)(w / 4) * (h / 4);
+	const long long threads = nb * 16;
+	KDecode<<<unsigned((threads + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d_blocks, d_bgra, stride, w / 4, int(nb));
+	CK(cudaGetLastError());
+	return NEBC7_OK;
+}
+
+int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n)
+{
+	if (n < 0)
+		return SetError(NEBC7_EINVAL);
+	if (n == 0)
+		return NEBC7_OK;
+	uint8_t *db = nullptr, *dp = nullptr;
+	if (cudaMalloc(&db, size_t(n) * 16) != cudaSuccess || cudaMalloc(&dp, size_t(n) * 64) != cudaSuccess)
+	{
+		cudaFree(db);
+		return SetError(NEBC7_ENOMEM);
+	}
+	int rc = NEBC7_OK;
+	if (cudaMemcpy(db, blocks, size_t(n) * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	if (rc == NEBC7_OK)
+		rc = nebc7_decode_device(db, dp, 16, 4, 4 * n, nullptr);
+	if (rc == NEBC7_OK && cudaMemcpy(bgra, dp, size_t(n) * 64, cudaMemcpyDeviceToHost) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	cudaFree(db);
+	cudaFree(dp);
+	return rc;
+}
+
+int nebc7_init_device(int denoise)
+{
+	if (denoise != 0 && denoise != 1)
+		return SetError(NEBC7_EINVAL);
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	const LevelTables* T = nullptr;
+	return BuildTables(dev, denoise, &T);
+}
+
+int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)
+{
+	int dev = 0, sms = 0, perSm = 0;
+	CK(cudaGetDevice(&dev));
+	CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KEncode<1>, kWarpsPerCta * 32, 0));
+	if (ctas_per_sm)
+		*ctas_per_sm = perSm;
+	if (warps_per_cta)
+		*warps_per_cta = kWarpsPerCta;
+	if (sm_count)
+		*sm_count = sms;
+	return NEBC7_OK;
+}
+
+} // extern "C"

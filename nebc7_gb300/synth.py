@@ -241,3 +241,66 @@ def image_for(kind: str, w: int, h: int, seed: int) -> np.ndarray:
     if kind == "alpha_blobs":
         return alpha_blobs(w, h, seed)
     raise ValueError(f"unknown synthetic image kind {kind!r}")
+
+
+def random_blocks(n: int, seed: int):
+    """n independent 4x4 cells for block-level parity tests.
+
+    Returns (cells, masks): uint8[n, 64] BGRA pixels (4 rows of 4) and
+    uint8[n, 64] masks (bytes A,G,R,B per pixel).  Mixes noise, gradients,
+    few-colour and edge blocks, near-solid and low-contrast blocks, opaque
+    and translucent alpha, and masks with invisible pixels, all-invisible
+    colour and arbitrary mask bytes.
+    """
+    rng = SplitMix64(seed)
+    cells = np.zeros((n, 16, 4), dtype=np.int64)
+    masks = np.full((n, 16, 4), 255, dtype=np.int64)
+    kinds = rng.below(8, n)
+    alpha_modes = rng.below(4, n)
+    mask_modes = rng.below(7, n)
+    for k in range(n):
+        t = int(kinds[k])
+        if t == 0:
+            c = rng.below(256, 64).reshape(16, 4)
+        elif t in (1, 5):
+            a = rng.below(256, 4)
+            b = rng.below(256, 4)
+            wt = rng.below(65, 16) if t == 5 else (np.arange(16) * 64) // 15
+            c = (a[None, :] * (64 - wt[:, None]) + b[None, :] * wt[:, None] + 32) >> 6
+            amp = 8 if t == 5 else 2
+            c = c + rng.between(-amp, amp, 64).reshape(16, 4)
+        elif t in (2, 4, 6):
+            npal = {2: int(rng.between(1, 3, 1)[0]), 4: 2, 6: 3}[t]
+            pal = rng.below(256, 4 * npal).reshape(npal, 4)
+            sel = rng.below(npal, 16)
+            c = pal[sel]
+            if t != 2:
+                c = c + rng.between(-3, 3, 64).reshape(16, 4)
+        elif t == 3:
+            c = rng.below(256, 4)[None, :] + rng.between(-1, 1, 64).reshape(16, 4)
+        else:
+            c = rng.below(256, 4)[None, :] + rng.between(-6, 6, 64).reshape(16, 4)
+        c = np.clip(c, 0, 255)
+        am = int(alpha_modes[k])
+        if am == 0:
+            c[:, 3] = 255
+        elif am == 1:
+            c[:, 3] = 255 - rng.below(20, 16)
+        cells[k] = c
+        mm = int(mask_modes[k])
+        if mm == 0:
+            inv = rng.below(256, 16) < int(rng.below(256, 1)[0])
+            masks[k, inv, 1:] = 0
+        elif mm == 1:
+            masks[k, :, 1:] = 0
+        elif mm == 2:
+            masks[k] = np.where(rng.below(5, 64).reshape(16, 4) == 0, 0, 255)
+        elif mm == 3:
+            masks[k] = rng.below(256, 64).reshape(16, 4)
+    return cells.reshape(n, 64).astype(np.uint8), masks.reshape(n, 64).astype(np.uint8)
+
+
+def random_start_blocks(n: int, seed: int) -> np.ndarray:
+    """n arbitrary 16-byte starting blocks (any mode, any bits)."""
+    rng = SplitMix64(seed)
+    return rng.below(256, n * 16).reshape(n, 16).astype(np.uint8)

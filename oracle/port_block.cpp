@@ -327,12 +327,14 @@ static void MakeCell(Cell& input, const Cell& decoded)
 	{
 		for (int c = 0; c < 4; c++)
 		{
-			const uint16_t m = input.msk[i][c] ? 0xFFFF : 0;
+			/* _mm_cvtepi8_epi16 of the mask byte: 0xFF -> 0xFFFF */
+			const uint16_t m = uint16_t(int16_t(int8_t(input.msk[i][c])));
 			const uint16_t v = uint16_t(input.img[i][c] & m);
 			input.px[i][c] = v;
 			input.mk[i][c] = m;
 		}
-		flags |= ((input.mk[i][1] & 1) << i);
+		/* bit i of the widened G mask, :72-76 */
+		flags |= ((input.mk[i][1] >> i) & 1) << i;
 		m0 &= input.px[i][0];
 	}
 	input.visibleFlags = flags;

@@ -1136,7 +1136,7 @@ void CompareBlocks(const Config& cfg, const Cell& a, const Cell& b, int& alpha, 
 		for (int c = 0; c < 4; c++)
 		{
 			int q = cfg.Q(int(a.img[i][c]) - int(b.img[i][c]));
-			q &= a.msk[i][c] ? 0xFFFF : 0;
+			q &= uint16_t(int16_t(int8_t(a.msk[i][c])));
 			sum[c] += q * q;
 		}
 	const int w[4] = { cfg.wA, cfg.wG, cfg.wR, cfg.wB };
