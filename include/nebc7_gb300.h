@@ -140,7 +140,8 @@ int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
 /* Builds the level tables of `denoise` on the current device ahead of use. */
 int nebc7_init_device(int denoise);
 
-/* Persistent-grid sizing of the encode kernel: CTAs per SM and warps per CTA. */
+/* Persistent-grid sizing of the encode kernel with the refinement passes
+   (the largest instantiation): CTAs per SM and warps per CTA. */
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);
 
 #ifdef __cplusplus

@@ -50,9 +50,23 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     with _lock:
         if not force and not needs_build():
             return LIB
-        LIBDIR.mkdir(exist_ok=True)
+        objdir = LIBDIR / "obj"
+        objdir.mkdir(parents=True, exist_ok=True)
+        # one translation unit per encode instantiation: compiled in parallel
+        procs = []
+        objs = []
+        for src in sorted(CSRC.glob("*.cu")):
+            obj = objdir / (src.stem + ".o")
+            cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+            if verbose:
+                print(" ".join(cmd), flush=True)
+            procs.append((src, subprocess.Popen(cmd)))
+            objs.append(obj)
+        failed = [src.name for src, p in procs if p.wait() != 0]
+        if failed:
+            raise RuntimeError(f"nvcc failed on {', '.join(failed)}")
         tmp = LIB.with_suffix(".so.tmp")
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-shared", str(CSRC / "nebc7_capi.cu"), "-o", str(tmp)]
+        cmd = [nvcc(), *ARCH, "-shared", *map(str, objs), "-o", str(tmp)]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -143,7 +143,7 @@ __device__ __forceinline__ int IndexAt(uint64_t lo, uint64_t hi, int start, int 
 
 /* Decodes the whole block: header into regs (best endpoints, parameter,
    mode) and pixel `pix` into out[4] (A,G,R,B).  Every lane can call it. */
-__device__ void DecodeBlock(uint64_t lo, uint64_t hi, int pix, uint8_t out[4], Ep best[3], int& param, int& mode)
+__device__ inline void DecodeBlock(uint64_t lo, uint64_t hi, int pix, uint8_t out[4], Ep best[3], int& param, int& mode)
 {
 	const int encoded = int(lo & 0xFF);
 	mode = 8;
@@ -319,7 +319,7 @@ __device__ void DecodeBlock(uint64_t lo, uint64_t hi, int pix, uint8_t out[4], E
 
 /* Warp: decodes the block into st.dec (lanes 0..15 one pixel each); returns
    the header in every lane. */
-__device__ void DecodeToState(WarpState& st, uint64_t lo, uint64_t hi, Ep best[3], int& param, int& mode, int lane)
+__device__ inline void DecodeToState(WarpState& st, uint64_t lo, uint64_t hi, Ep best[3], int& param, int& mode, int lane)
 {
 	uint8_t px[4];
 	DecodeBlock(lo, hi, lane & 15, px, best, param, mode);
@@ -375,7 +375,7 @@ __device__ __forceinline__ double SsimRatio(int sasb, int sab, int sasa_sbsb, in
 	return __ddiv_rn(num, den);
 }
 
-__device__ void CompareBlocksSSIM(const WarpState& st, const Params& P, int lane, double& alpha, double& color)
+__device__ inline void CompareBlocksSSIM(const WarpState& st, const Params& P, int lane, double& alpha, double& color)
 {
 	double r[4];
 	for (int c = 0; c < 4; c++)
@@ -441,7 +441,7 @@ __device__ __forceinline__ void SwapPair(uint16_t* b, int lane)
 
 /* Bounds, counts and channel orientation of the pixel subset `member`
    (bit i = pixel i); order-independent, so a lane can evaluate any subset. */
-__device__ AreaInfo AreaStats(const WarpState& st, const CellRegs& R, const Params& P, uint32_t member)
+__device__ inline AreaInfo AreaStats(const WarpState& st, const CellRegs& R, const Params& P, uint32_t member)
 {
 	AreaInfo a;
 	const uint32_t vis = member & R.visible;
@@ -624,7 +624,7 @@ __device__ AreaInfo AreaStats(const WarpState& st, const CellRegs& R, const Para
 /* Writes the ordered pixel list of a subset into `ar` (lanes 0..15).
    `anchor` is the subset's first pixel; members follow in ascending order,
    visible pixels first. */
-__device__ void BuildAreaList(Area& ar, const WarpState& st, const CellRegs& R, uint32_t member, int anchor, int lane)
+__device__ inline void BuildAreaList(Area& ar, const WarpState& st, const CellRegs& R, uint32_t member, int anchor, int lane)
 {
 	uint32_t rest = member & ~(1u << anchor);
 	/* position of every member in the selection order */

@@ -12,12 +12,12 @@
 
 namespace nebc7 {
 
-__constant__ int c_interp2[4] = { 0, 21, 43, 64 };
-__constant__ int c_interp3[8] = { 0, 9, 18, 27, 37, 46, 55, 64 };
-__constant__ int c_interp4[16] = { 0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64 };
+static __constant__ int c_interp2[4] = { 0, 21, 43, 64 };
+static __constant__ int c_interp3[8] = { 0, 9, 18, 27, 37, 46, 55, 64 };
+static __constant__ int c_interp4[16] = { 0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64 };
 
 /* subset of pixel i in partition p: (c_part[p] >> 2i) & 3 */
-__constant__ uint32_t c_part2[64] = {
+static __constant__ uint32_t c_part2[64] = {
 	0x50505050u, 0x40404040u, 0x54545454u, 0x54505040u, 0x50404000u, 0x55545450u, 0x55545040u, 0x54504000u,
 	0x50400000u, 0x55555450u, 0x55544000u, 0x54400000u, 0x55555440u, 0x55550000u, 0x55555500u, 0x55000000u,
 	0x55150100u, 0x00004054u, 0x15010000u, 0x00405054u, 0x00004050u, 0x15050100u, 0x05010000u, 0x40505054u,
@@ -27,7 +27,7 @@ __constant__ uint32_t c_part2[64] = {
 	0x00041504u, 0x00105410u, 0x10541000u, 0x04150400u, 0x50410514u, 0x41051450u, 0x05415014u, 0x14054150u,
 	0x41050514u, 0x41505014u, 0x40011554u, 0x54150140u, 0x50505500u, 0x00555050u, 0x15151010u, 0x54540404u,
 };
-__constant__ uint32_t c_part3[64] = {
+static __constant__ uint32_t c_part3[64] = {
 	0xAA685050u, 0x6A5A5040u, 0x5A5A4200u, 0x5450A0A8u, 0xA5A50000u, 0xA0A05050u, 0x5555A0A0u, 0x5A5A5050u,
 	0xAA550000u, 0xAA555500u, 0xAAAA5500u, 0x90909090u, 0x94949494u, 0xA4A4A4A4u, 0xA9A59450u, 0x2A0A4250u,
 	0xA5945040u, 0x0A425054u, 0xA5A5A500u, 0x55A0A0A0u, 0xA8A85454u, 0x6A6A4040u, 0xA4A45000u, 0x1A1A0500u,
@@ -37,21 +37,21 @@ __constant__ uint32_t c_part3[64] = {
 	0xAA444444u, 0x54A854A8u, 0x95809580u, 0x96969600u, 0xA85454A8u, 0x80959580u, 0xAA141414u, 0x96960000u,
 	0xAAAA1414u, 0xA05050A0u, 0xA0A5A5A0u, 0x96000000u, 0x40804080u, 0xA9A8A9A8u, 0xAAAAAA44u, 0x2A4A5254u,
 };
-__constant__ uint8_t c_anchor22[64] = {
+static __constant__ uint8_t c_anchor22[64] = {
 	15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 2, 8, 2, 2, 8, 8, 15, 2, 8, 2, 2, 8, 8, 2, 2,
 	15, 15, 6, 8, 2, 8, 15, 15, 2, 8, 2, 2, 2, 15, 15, 6, 6, 2, 6, 8, 15, 15, 2, 2, 15, 15, 15, 15, 15, 2, 2, 15,
 };
-__constant__ uint8_t c_anchor23[64] = {
+static __constant__ uint8_t c_anchor23[64] = {
 	3, 3, 15, 15, 8, 3, 15, 15, 8, 8, 6, 6, 6, 5, 3, 3, 3, 3, 8, 15, 3, 3, 6, 10, 5, 8, 8, 6, 8, 5, 15, 15,
 	8, 15, 3, 5, 6, 10, 8, 15, 15, 3, 15, 5, 15, 15, 15, 15, 3, 15, 5, 5, 5, 8, 5, 10, 5, 10, 8, 13, 15, 12, 3, 3,
 };
-__constant__ uint8_t c_anchor33[64] = {
+static __constant__ uint8_t c_anchor33[64] = {
 	15, 8, 8, 3, 15, 15, 3, 8, 15, 15, 15, 15, 15, 15, 15, 8, 15, 8, 15, 3, 15, 8, 15, 8, 3, 15, 6, 10, 15, 15, 10, 8,
 	15, 3, 15, 10, 10, 8, 9, 10, 6, 15, 8, 15, 3, 6, 6, 8, 15, 3, 15, 15, 15, 15, 15, 15, 15, 15, 15, 15, 3, 15, 15, 8,
 };
 /* rotation visiting orders, mode 4 (rotation | idxMode << 2) and mode 5 */
-__constant__ int c_rot4[8] = { 4, 0, 6, 2, 5, 1, 7, 3 };
-__constant__ int c_rot5[4] = { 0, 2, 1, 3 };
+static __constant__ int c_rot4[8] = { 4, 0, 6, 2, 5, 1, 7, 3 };
+static __constant__ int c_rot5[4] = { 0, 2, 1, 3 };
 
 /* Level tables for one kDenoise value, resident in device memory (layouts
    and contents as described in the table builder). */

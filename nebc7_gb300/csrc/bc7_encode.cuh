@@ -40,8 +40,8 @@ struct Job
 
 constexpr int kWarpsPerCta = 4;
 
-template<int kD>
-__device__ void EncodeBlock(WarpState& st, const Job& job, const LevelTables& T, const Params& P, int k, int lane)
+template<int kD, bool NORMAL>
+__device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T, const Params& P, int k, int lane)
 {
 	const int bx = k % job.blocksW, by = k / job.blocksW;
 	const long long base = (long long)by * 4 * job.stride + (long long)bx * 16;
@@ -169,8 +169,8 @@ __device__ void EncodeBlock(WarpState& st, const Job& job, const LevelTables& T,
 				}
 			}
 
-			if (P.doNormal)
-				NormalPasses<kD>(st, R, P, T, job.status, lane);
+			if (NORMAL)
+				NormalPasses<kD>(st, *ss, R, P, T, lane);
 
 			if (water > R.errTotal)
 				FinalPack<kD>(st, R, P, lo, hi, lane);
@@ -208,12 +208,16 @@ __device__ void EncodeBlock(WarpState& st, const Job& job, const LevelTables& T,
 	__syncwarp();
 }
 
-template<int kD>
+/* NORMAL selects the refinement / full-search passes; only that
+   instantiation reserves the per-warp search state in shared memory. */
+template<int kD, bool NORMAL>
 __global__ void __launch_bounds__(kWarpsPerCta * 32) KEncode(Job job, LevelTables T, Params P)
 {
 	__shared__ WarpState states[kWarpsPerCta];
+	__shared__ __align__(16) unsigned char searchRaw[NORMAL ? kWarpsPerCta * sizeof(SearchState) : 16];
 	const int lane = threadIdx.x & 31;
 	WarpState& st = states[threadIdx.x >> 5];
+	SearchState* ss = NORMAL ? reinterpret_cast<SearchState*>(searchRaw) + (threadIdx.x >> 5) : nullptr;
 	for (;;)
 	{
 		int k = 0;
@@ -222,69 +226,17 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) KEncode(Job job, LevelTable
 		k = __shfl_sync(kFull, k, 0);
 		if (k >= job.nblocks)
 			break;
-		EncodeBlock<kD>(st, job, T, P, k, lane);
+		EncodeBlock<kD, NORMAL>(st, ss, job, T, P, k, lane);
 	}
 }
 
-/* Decodes blocks to BGRA pixels (src/Bc7Core.cpp:1904 DecompressKernel):
-   one thread per pixel. */
-__global__ void KDecode(const uint8_t* blocks, uint8_t* bgra, long long stride, int blocksW, int nblocks)
-{
-	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-	if (t >= (long long)nblocks * 16)
-		return;
-	const int k = int(t >> 4), i = int(t & 15);
-	const uint4 b = *reinterpret_cast<const uint4*>(blocks + (long long)k * 16);
-	const uint64_t lo = uint64_t(b.x) | (uint64_t(b.y) << 32);
-	const uint64_t hi = uint64_t(b.z) | (uint64_t(b.w) << 32);
-	uint8_t px[4];
-	Ep best[3];
-	int param, mode;
-	DecodeBlock(lo, hi, i, px, best, param, mode);
-	const int bx = k % blocksW, by = k / blocksW;
-	uint8_t* p = bgra + ((long long)by * 4 + (i >> 2)) * stride + (long long)bx * 16 + (i & 3) * 4;
-	*reinterpret_cast<uchar4*>(p) = make_uchar4(px[3], px[1], px[2], px[0]);
-}
+/* Host-side launchers of KEncode.  Each instantiation is compiled in a
+   translation unit of its own (encode_d<kD>_<passes>.cu), so the four build
+   in parallel; the C ABI layer only sees these declarations. */
+template<int kD, bool NORMAL>
+cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T, const Params& P);
 
-/* Deterministic reduction of the per-block results: a fixed-shape tree, so
-   repeated runs give identical double sums. */
-__global__ void KReduceResults(const BlockResult* r, int n, long long* errs, double* ssims)
-{
-	__shared__ long long sa[256], sc[256];
-	__shared__ double qa[256], qc[256];
-	const int t = threadIdx.x;
-	long long a = 0, c = 0;
-	double x = 0, y = 0;
-	for (int i = t; i < n; i += 256)
-	{
-		a += r[i].errAlpha;
-		c += r[i].errColor;
-		x = __dadd_rn(x, r[i].ssimAlpha);
-		y = __dadd_rn(y, r[i].ssimColor);
-	}
-	sa[t] = a;
-	sc[t] = c;
-	qa[t] = x;
-	qc[t] = y;
-	__syncthreads();
-	for (int s = 128; s > 0; s >>= 1)
-	{
-		if (t < s)
-		{
-			sa[t] += sa[t + s];
-			sc[t] += sc[t + s];
-			qa[t] = __dadd_rn(qa[t], qa[t + s]);
-			qc[t] = __dadd_rn(qc[t], qc[t + s]);
-		}
-		__syncthreads();
-	}
-	if (t == 0)
-	{
-		errs[0] = sa[0];
-		errs[1] = sc[0];
-		ssims[0] = qa[0];
-		ssims[1] = qc[0];
-	}
-}
+template<int kD, bool NORMAL>
+cudaError_t EncodeKernelOccupancy(int* ctasPerSm);
 
 } // namespace nebc7

@@ -1,0 +1,4 @@
+/* KEncode instantiation: exact differences (kDenoise 0), draft passes only. */
+#include "bc7_encode_entry.cuh"
+
+NEBC7_INSTANTIATE_ENCODE(0, false)

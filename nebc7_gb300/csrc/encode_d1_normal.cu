@@ -1,0 +1,4 @@
+/* KEncode instantiation: differences halved (kDenoise 1), draft, refinement and full-search passes. */
+#include "bc7_encode_entry.cuh"
+
+NEBC7_INSTANTIATE_ENCODE(1, true)

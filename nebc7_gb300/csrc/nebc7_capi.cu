@@ -7,7 +7,7 @@
  * the reference's IBc7Core / ProcessTexture interfaces onto it.
  */
 #include "bc7_tables.cuh"
-#include "bc7_encode.cuh"
+#include "bc7_decode.cuh"
 
 #include "../../include/nebc7_gb300.h"
 
@@ -155,7 +155,38 @@ int ValidateSettings(const nebc7_settings* s)
 	return NEBC7_OK;
 }
 
-int GridFor(int nblocks)
+/* The four encode instantiations: denoise shift x refinement passes. */
+struct EncodeVariant
+{
+	cudaError_t (*launch)(int, cudaStream_t, const Job&, const LevelTables&, const Params&);
+	cudaError_t (*occupancy)(int*);
+};
+
+const EncodeVariant kVariants[4] = {
+	{ LaunchEncodeKernel<0, false>, EncodeKernelOccupancy<0, false> },
+	{ LaunchEncodeKernel<0, true>, EncodeKernelOccupancy<0, true> },
+	{ LaunchEncodeKernel<1, false>, EncodeKernelOccupancy<1, false> },
+	{ LaunchEncodeKernel<1, true>, EncodeKernelOccupancy<1, true> },
+};
+
+int VariantSlot(int denoise, bool normal) { return (denoise ? 2 : 0) + (normal ? 1 : 0); }
+
+/* Resident CTAs per SM of one encode instantiation (cached per process;
+   every device of a process is the same GB300 part). */
+int CtasPerSm(int denoise, bool normal)
+{
+	static int cache[4] = { 0, 0, 0, 0 };
+	const int slot = VariantSlot(denoise, normal);
+	if (!cache[slot])
+	{
+		int perSm = 0;
+		kVariants[slot].occupancy(&perSm);
+		cache[slot] = perSm > 0 ? perSm : 1;
+	}
+	return cache[slot];
+}
+
+int GridFor(int nblocks, int denoise, bool normal)
 {
 	static int sms = 0;
 	if (!sms)
@@ -166,10 +197,7 @@ int GridFor(int nblocks)
 		if (sms <= 0)
 			sms = 1;
 	}
-	int perSm = 0;
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KEncode<1>, kWarpsPerCta * 32, 0);
-	if (perSm <= 0)
-		perSm = 1;
+	const int perSm = CtasPerSm(denoise, normal);
 	const int ctasNeeded = (nblocks + kWarpsPerCta - 1) / kWarpsPerCta;
 	const int g = sms * perSm;
 	return ctasNeeded < g ? ctasNeeded : g;
@@ -217,12 +245,9 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 	job.counter = counter;
 	job.status = status;
 	const Params P = MakeParams(s);
-	const int grid = GridFor(nblocks);
-	if (s.denoise)
-		KEncode<1><<<grid, kWarpsPerCta * 32, 0, stream>>>(job, *T, P);
-	else
-		KEncode<0><<<grid, kWarpsPerCta * 32, 0, stream>>>(job, *T, P);
-	CK(cudaGetLastError());
+	const bool normal = s.doNormal != 0;
+	const int grid = GridFor(nblocks, s.denoise, normal);
+	CK(kVariants[VariantSlot(s.denoise, normal)].launch(grid, stream, job, *T, P));
 
 	int rc = NEBC7_OK;
 	if (wantSums)
@@ -526,7 +551,7 @@ int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)
 	int dev = 0, sms = 0, perSm = 0;
 	CK(cudaGetDevice(&dev));
 	CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, KEncode<1>, kWarpsPerCta * 32, 0));
+	CK(kVariants[VariantSlot(1, true)].occupancy(&perSm));
 	if (ctas_per_sm)
 		*ctas_per_sm = perSm;
 	if (warps_per_cta)
