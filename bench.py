@@ -27,7 +27,6 @@ import ctypes
 import hashlib
 import json
 import os
-import subprocess
 import sys
 import threading
 import time
@@ -64,58 +63,76 @@ def prepare(name):
     return padded, mask, o, d, s, gkey
 
 
-class ClockSampler:
-    """Samples SM clocks and throttle reasons while the timed region runs."""
+class NvmlSampler:
+    """Samples the SM clock and the clock-event (throttle) reasons every few
+    milliseconds through NVML (read-only queries), so that even a short timed
+    region gets samples."""
 
-    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
-             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    BITS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
 
-    def __init__(self, index: int):
-        self.index = index
-        self.proc = None
-        self.lines = []
+    def __init__(self, device, period_s: float = 0.005):
+        self.period = period_s
+        self.samples = []
+        self.max_mhz = None
+        self.ok = False
+        self.stop = threading.Event()
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            handle = ctypes.c_void_p()
+            bus = self._bus_id(device)
+            rc = -1
+            if bus:
+                rc = nv.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(handle))
+            if rc != 0:
+                rc = nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device.index or 0), ctypes.byref(handle))
+            if rc != 0:
+                return
+            self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self.nv, self.handle, self.ok = nv, handle, True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    @staticmethod
+    def _bus_id(device):
+        try:
+            import torch
+            p = torch.cuda.get_device_properties(device)
+            return f"{p.pci_domain_id:08X}:{p.pci_bus_id:02X}:{p.pci_device_id:02X}.0"
+        except Exception:
+            return None
+
+    def _run(self):
+        mhz = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        while not self.stop.is_set():
+            if self.nv.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.handle, ctypes.byref(rs)) == 0:
+                self.samples.append((float(mhz.value), int(rs.value)))
+            self.stop.wait(self.period)
 
     def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self.thread = threading.Thread(target=self._read, daemon=True)
+        if self.ok:
+            self.thread = threading.Thread(target=self._run, daemon=True)
             self.thread.start()
-        except OSError:
-            self.proc = None
         return self
 
-    def _read(self):
-        for line in self.proc.stdout:
-            self.lines.append(line.strip())
-
     def __exit__(self, *a):
-        if self.proc:
-            self.proc.terminate()
-            try:
-                self.proc.wait(timeout=5)
-            except subprocess.TimeoutExpired:
-                self.proc.kill()
+        if self.ok:
+            self.stop.set()
+            self.thread.join(timeout=2)
 
     def summary(self):
-        sm, mx, reasons = [], 0.0, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
-            parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 8:
-                continue
-            try:
-                sm.append(float(parts[0]))
-                mx = max(mx, float(parts[1]))
-            except ValueError:
-                continue
-            for n, v in zip(names, parts[4:8]):
-                if v.lower().startswith("active"):
-                    reasons.add(n)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["unsampled"], "samples": 0}
+        reasons = sorted({n for _, r in self.samples for b, n in self.BITS.items() if r & b})
+        return {"sm_mhz": float(np.median([m for m, _ in self.samples])), "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.samples), "source": "nvml"}
 
 
 def cpu_rate(padded, mask, o, d, s, budget_s=12.0, threads=None):
@@ -218,7 +235,7 @@ def run_ours(args, rank, world, local):
         dist.barrier()
     torch.cuda.synchronize()
     wall0 = time.time()
-    with ClockSampler(local) as clocks:
+    with NvmlSampler(dev) as clocks:
         for i in range(args.steps):
             flush.zero_()
             starts[i].record(stream)
@@ -299,7 +316,7 @@ def run_ours(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)

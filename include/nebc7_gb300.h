@@ -120,7 +120,11 @@ typedef struct nebc7_settings
 int nebc7_encode_device(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w, int h,
 	const nebc7_settings* settings, int64_t* errs, double* ssim, void* stream);
 
-/* Same with host buffers: copies in, encodes, copies the blocks back. */
+/* Same with host buffers: copies in, encodes, copies the blocks back, and
+   waits.  Device staging buffers are cached per device and per concurrent
+   caller for the life of the process (they only grow), so repeated calls do
+   not allocate; pinned host buffers give the fastest copies.  Safe to call
+   from several threads at once. */
 int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int w, int h,
 	const nebc7_settings* settings, int64_t* errs, double* ssim);
 

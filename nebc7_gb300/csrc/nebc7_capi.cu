@@ -203,9 +203,18 @@ int GridFor(int nblocks, int denoise, bool normal)
 	return ctasNeeded < g ? ctasNeeded : g;
 }
 
-/* Enqueues one encode over `nblocks` blocks described by job geometry. */
+/* Scratch of one encode: the work-queue head and status word, the reduced
+   sums and, when sums are wanted, one BlockResult per block. */
+size_t EncodeScratchBytes(int nblocks, bool wantSums)
+{
+	return 256 + (wantSums ? size_t(nblocks) * sizeof(BlockResult) : 0) + 64;
+}
+
+/* Enqueues one encode.  `scratchIn` (EncodeScratchBytes bytes, 256-byte
+   aligned) is used when given, otherwise the scratch is taken from the
+   stream-ordered allocator. */
 int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int blocksW, int nblocks,
-	const nebc7_settings& s, int64_t* errs, double* ssim, cudaStream_t stream)
+	const nebc7_settings& s, int64_t* errs, double* ssim, cudaStream_t stream, uint8_t* scratchIn = nullptr)
 {
 	if (nblocks <= 0)
 	{
@@ -222,10 +231,8 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 		return e;
 
 	const bool wantSums = errs || ssim;
-	const size_t resBytes = wantSums ? size_t(nblocks) * sizeof(BlockResult) : 0;
-	const size_t scratchBytes = 256 + resBytes + 64;
-	uint8_t* scratch = nullptr;
-	if (cudaMallocAsync((void**)&scratch, scratchBytes, stream) != cudaSuccess)
+	uint8_t* scratch = scratchIn;
+	if (!scratch && cudaMallocAsync((void**)&scratch, EncodeScratchBytes(nblocks, wantSums), stream) != cudaSuccess)
 		return SetError(NEBC7_ENOMEM);
 	int* counter = (int*)scratch;
 	int* status = counter + 1;
@@ -273,9 +280,73 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 		if (hstatus)
 			rc = SetError(NEBC7_ELIMIT);
 	}
-	CK(cudaFreeAsync(scratch, stream));
+	if (!scratchIn)
+		CK(cudaFreeAsync(scratch, stream));
 	return rc;
 }
+
+/* ---- staging for the host-buffer entries ------------------------------- */
+
+/* One staging slot: a device buffer that only grows and a stream of its own.
+   Concurrent host calls (the reference's worker threads) each take a free
+   slot, so their copies and kernels overlap; slots live for the process. */
+struct HostSlot
+{
+	int device;
+	cudaStream_t stream;
+	uint8_t* buf;
+	size_t cap;
+};
+
+std::mutex gSlotMutex;
+std::vector<HostSlot*> gFreeSlots;
+
+HostSlot* AcquireSlot(int dev)
+{
+	{
+		std::lock_guard<std::mutex> lock(gSlotMutex);
+		for (size_t i = 0; i < gFreeSlots.size(); i++)
+			if (gFreeSlots[i]->device == dev)
+			{
+				HostSlot* h = gFreeSlots[i];
+				gFreeSlots.erase(gFreeSlots.begin() + i);
+				return h;
+			}
+	}
+	HostSlot* h = new HostSlot{ dev, nullptr, nullptr, 0 };
+	if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+	{
+		delete h;
+		return nullptr;
+	}
+	return h;
+}
+
+void ReleaseSlot(HostSlot* h)
+{
+	std::lock_guard<std::mutex> lock(gSlotMutex);
+	gFreeSlots.push_back(h);
+}
+
+bool ReserveSlot(HostSlot* h, size_t bytes)
+{
+	if (bytes <= h->cap)
+		return true;
+	if (h->buf)
+	{
+		cudaStreamSynchronize(h->stream);
+		cudaFree(h->buf);
+		h->buf = nullptr;
+		h->cap = 0;
+	}
+	const size_t want = bytes + bytes / 4;
+	if (cudaMalloc((void**)&h->buf, want) != cudaSuccess)
+		return false;
+	h->cap = want;
+	return true;
+}
+
+inline size_t Align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 /* ---- IBc7Core adapter ------------------------------------------------- */
 
@@ -444,24 +515,36 @@ int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, lo
 		return SetError(NEBC7_EINVAL);
 	const size_t nb = size_t(w / 4) * (h / 4);
 	const size_t img = size_t(w) * 4 * h;
-	uint8_t *dd = nullptr, *db = nullptr, *dm = nullptr;
-	if (cudaMalloc(&dd, nb * 16) != cudaSuccess || cudaMalloc(&db, img) != cudaSuccess || (mask && cudaMalloc(&dm, img) != cudaSuccess))
+	if (nb > size_t(0x7FFFFFFF))
+		return SetError(NEBC7_ETOOBIG);
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	HostSlot* slot = AcquireSlot(dev);
+	if (!slot)
+		return SetError(NEBC7_ECUDA);
+	const size_t offImg = Align256(nb * 16);
+	const size_t offMask = offImg + Align256(img);
+	const size_t offScratch = offMask + (mask ? Align256(img) : 0);
+	if (!ReserveSlot(slot, offScratch + EncodeScratchBytes(int(nb), true)))
 	{
-		cudaFree(dd);
-		cudaFree(db);
-		cudaFree(dm);
+		ReleaseSlot(slot);
 		return SetError(NEBC7_ENOMEM);
 	}
+	cudaStream_t st = slot->stream;
+	uint8_t* dd = slot->buf;
+	uint8_t* db = slot->buf + offImg;
+	uint8_t* dm = mask ? slot->buf + offMask : nullptr;
 	int rc = NEBC7_OK;
-	if (cudaMemcpy2D(db, size_t(w) * 4, bgra, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice) != cudaSuccess ||
-		(mask && cudaMemcpy2D(dm, size_t(w) * 4, mask, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice) != cudaSuccess) ||
-		cudaMemcpy(dd, dst, nb * 16, cudaMemcpyHostToDevice) != cudaSuccess)
+	if (cudaMemcpy2DAsync(db, size_t(w) * 4, bgra, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+		(mask && cudaMemcpy2DAsync(dm, size_t(w) * 4, mask, size_t(stride), size_t(w) * 4, size_t(h), cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+		cudaMemcpyAsync(dd, dst, nb * 16, cudaMemcpyHostToDevice, st) != cudaSuccess)
 		rc = SetError(NEBC7_ECUDA);
 	int64_t e[2];
 	double q[2];
 	if (rc == NEBC7_OK)
-		rc = LaunchEncode(dd, db, dm, (long long)w * 4, w / 4, int(nb), *settings, e, q, nullptr);
-	if (rc == NEBC7_OK && cudaMemcpy(dst, dd, nb * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+		rc = LaunchEncode(dd, db, dm, (long long)w * 4, w / 4, int(nb), *settings, e, q, st, slot->buf + offScratch);
+	if (rc == NEBC7_OK && (cudaMemcpyAsync(dst, dd, nb * 16, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+		cudaStreamSynchronize(st) != cudaSuccess))
 		rc = SetError(NEBC7_ECUDA);
 	if (rc == NEBC7_OK)
 	{
@@ -476,9 +559,9 @@ int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, lo
 			ssim[1] = q[1];
 		}
 	}
-	cudaFree(dd);
-	cudaFree(db);
-	cudaFree(dm);
+	else
+		cudaStreamSynchronize(st);
+	ReleaseSlot(slot);
 	return rc;
 }
 
