@@ -144,6 +144,30 @@ int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
 /* Builds the level tables of `denoise` on the current device ahead of use. */
 int nebc7_init_device(int denoise);
 
+/* Allocation-free variant of nebc7_encode_device (no counterpart in the
+   reference, whose CPU encoder needs no device memory).  For callers that
+   cannot let the library allocate device memory while they run: a serving
+   loop that admits jobs against a fixed HBM budget, or a loop that must not
+   meet the device-wide synchronisation cudaMalloc / cudaFree can cause.
+   The call itself makes no allocation of any kind.  Its scratch is one
+   fixed device array inside the library, sized for at most 65536 blocks
+   (a 1024x1024 texture); larger textures are rejected with NEBC7_ETOOBIG.
+   Setup: call nebc7_init_device(settings->denoise) on the device first (it
+   allocates the level tables; without it this call returns NEBC7_EINVAL).
+   The first call on each device looks up the scratch array's address with
+   that device current; make that first call before any stream capture.
+   Each call zeroes the scratch's work-queue head and status word on
+   `stream` before its kernel; nothing else needs to start at zero.
+   d_sums, if non-null (8-byte aligned device memory), receives
+   { int64 errAlpha, int64 errColor, double ssimAlpha, double ssimColor }
+   as nebc7_encode_device reports them.  The call only enqueues work and
+   never waits.  All calls on a device share the one scratch array, so calls
+   whose work overlaps on the device (different streams, or threads without
+   ordering) race and corrupt each other's results: issue them in one stream
+   or order them. */
+int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w,
+	int h, const nebc7_settings* settings, void* d_sums, void* stream);
+
 /* Persistent-grid sizing of the encode kernel with the refinement passes
    (the largest instantiation): CTAs per SM and warps per CTA. */
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);

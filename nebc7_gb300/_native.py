@@ -131,6 +131,7 @@ SIGNATURES = {
     "nebc7_decode_blocks_host": (I, [VP, VP, I]),
     "nebc7_init_device": (I, [I]),
     "nebc7_launch_shape": (I, [VP, VP, VP]),
+    "nebc7_encode_device_noalloc": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),
 }
 
 

@@ -425,7 +425,97 @@ int CoreWeightColor()
 
 } // namespace
 
+/* ---- allocation-free encode -------------------------------------------- */
+
+/* Largest texture nebc7_encode_device_noalloc accepts: 65536 blocks
+   (1024x1024 pixels).  Its scratch lives in this fixed device array instead
+   of coming from an allocator: 256 bytes for the work-queue head and the
+   status word, then one BlockResult per block for the error / SSIM sums. */
+constexpr int kNoAllocMaxBlocks = 65536;
+constexpr size_t kNoAllocScratchBytes = 256 + size_t(kNoAllocMaxBlocks) * sizeof(BlockResult);
+static __device__ __align__(256) unsigned char gNoAllocScratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex gNoAllocMutex;
+uint8_t* gNoAllocPtr[kMaxDevices] = {};
+
+/* Device address of gNoAllocScratch on `dev`, looked up once per device
+   (with that device current) and cached. */
+int NoAllocScratch(int dev, uint8_t** out)
+{
+	if (dev < 0 || dev >= kMaxDevices)
+		return SetError(NEBC7_EINVAL);
+	std::lock_guard<std::mutex> lock(gNoAllocMutex);
+	if (!gNoAllocPtr[dev])
+	{
+		void* p = nullptr;
+		if (cudaGetSymbolAddress(&p, gNoAllocScratch) != cudaSuccess || !p)
+			return SetError(NEBC7_ECUDA);
+		gNoAllocPtr[dev] = (uint8_t*)p;
+	}
+	*out = gNoAllocPtr[dev];
+	return NEBC7_OK;
+}
+
+/* The level tables of `denoise` on `dev` if they were already built, else null. */
+const LevelTables* BuiltTables(int dev, int denoise)
+{
+	std::lock_guard<std::mutex> lock(gMutex);
+	if (dev < 0 || dev >= kMaxDevices || !gTables[dev][denoise].built)
+		return nullptr;
+	return &gTables[dev][denoise].t;
+}
+
+} // namespace
+
 extern "C" {
+
+int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w,
+	int h, const nebc7_settings* settings, void* d_sums, void* stream)
+{
+	if (int e = ValidateSettings(settings))
+		return SetError(e);
+	if (w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4 || (stride & 3))
+		return SetError(NEBC7_EINVAL);
+	if (((uintptr_t)d_dst & 15) || ((uintptr_t)d_bgra & 3) || ((uintptr_t)d_mask & 3) || ((uintptr_t)d_sums & 7))
+		return SetError(NEBC7_EINVAL);
+	const long long nb = (long long)(w / 4) * (h / 4);
+	if (nb > kNoAllocMaxBlocks)
+		return SetError(NEBC7_ETOOBIG);
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	const LevelTables* T = BuiltTables(dev, settings->denoise);
+	if (!T)
+		return SetError(NEBC7_EINVAL);   /* nebc7_init_device(denoise) was not called on this device */
+	uint8_t* scratch = nullptr;
+	if (int e = NoAllocScratch(dev, &scratch))
+		return e;
+
+	const cudaStream_t st = (cudaStream_t)stream;
+	/* the queue head and status word must start at zero */
+	CK(cudaMemsetAsync(scratch, 0, 256, st));
+	Job job;
+	job.dst = d_dst;
+	job.bgra = d_bgra;
+	job.mask = d_mask;
+	job.stride = stride;
+	job.blocksW = w / 4;
+	job.nblocks = int(nb);
+	job.results = d_sums ? (BlockResult*)(scratch + 256) : nullptr;
+	job.counter = (int*)scratch;
+	job.status = (int*)scratch + 1;
+	const Params P = MakeParams(*settings);
+	const bool normal = settings->doNormal != 0;
+	CK(kVariants[VariantSlot(settings->denoise, normal)].launch(GridFor(int(nb), settings->denoise, normal), st, job, *T, P));
+	if (d_sums)
+	{
+		KReduceResults<<<1, 256, 0, st>>>(job.results, int(nb), (long long*)d_sums, (double*)((uint8_t*)d_sums + 16));
+		CK(cudaGetLastError());
+	}
+	return NEBC7_OK;
+}
+
 
 bool nebc7_GetBc7Core(void* bc7Core)
 {
