@@ -283,10 +283,16 @@ def run_ours(args, rank, world, local):
         peak, peak_src = 6800.0, "fallback"
     algo_bytes = nblocks * (64 + (64 if mask is not None else 0) + 16 + 16)
     achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
-    traffic = None
-    tf = ROOT / "profiles" / "encode_traffic.json"
+    # per-launch DRAM traffic and issue utilisation of the encode kernel, from the
+    # committed ncu capture of this workload (null when there is none)
+    traffic, issue = None, None
+    tf = ROOT / "profiles" / "kencode_ncu.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(args.workload)
+        prof = json.loads(tf.read_text()).get(args.workload)
+        if prof:
+            traffic = prof["dram_bytes_per_launch"]
+            issue = {k: prof[k] for k in ("sm_issue_active_pct_elapsed", "pipe_alu_pct_active", "pipe_fma_pct_active")}
+            issue["source"] = "profiles/" + prof["summary"]
 
     if rank == 0:
         cpu_value, cores, sample, _ = cpu_rate(padded, mask, o, d, s, budget_s=args.cpu_budget)
@@ -302,7 +308,9 @@ def run_ours(args, rank, world, local):
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src, "kernel_ms": kernel_ms,
-                         "note": "integer-issue bound search; HBM bytes are the algorithmic input/output bytes"},
+                         "algorithmic_bytes_per_block": algo_bytes // nblocks, "issue_ncu": issue,
+                         "note": "integer-issue and latency bound search; HBM bytes are the algorithmic "
+                                 "input/output bytes, of measured peak"},
             "cpu_baseline": {"value": cpu_value, "unit": "Mpx/s", "cores": cores, "kind": "port", "sample": sample},
             "clocks": clocks.summary(),
             "wall_s_timed": wall,
