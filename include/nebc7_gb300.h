@@ -154,8 +154,9 @@ int nebc7_init_device(int denoise);
    (a 1024x1024 texture); larger textures are rejected with NEBC7_ETOOBIG.
    Setup: call nebc7_init_device(settings->denoise) on the device first (it
    allocates the level tables; without it this call returns NEBC7_EINVAL).
-   The first call on each device looks up the scratch array's address with
-   that device current; make that first call before any stream capture.
+   The first call on each device does one-time setup with that device
+   current (it looks up the scratch array's address and sizes the kernel's
+   launch); make that first call before any stream capture.
    Each call zeroes the scratch's work-queue head and status word on
    `stream` before its kernel; nothing else needs to start at zero.
    d_sums, if non-null (8-byte aligned device memory), receives
@@ -168,8 +169,8 @@ int nebc7_init_device(int denoise);
 int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w,
 	int h, const nebc7_settings* settings, void* d_sums, void* stream);
 
-/* Persistent-grid sizing of the encode kernel with the refinement passes
-   (the largest instantiation): CTAs per SM and warps per CTA. */
+/* Persistent-grid sizing of the encode kernel of the default preset
+   (kDenoise 1 with the refinement passes): CTAs per SM and warps per CTA. */
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);
 
 #ifdef __cplusplus

@@ -63,7 +63,7 @@ struct AreaInfo
 	bool opaque;
 };
 
-struct WarpState
+struct __align__(16) WarpState
 {
 	uint8_t img[16][4];    /* source pixels, A,G,R,B */
 	uint8_t msk[16][4];    /* mask bytes, A,G,R,B */
@@ -441,7 +441,7 @@ __device__ __forceinline__ void SwapPair(uint16_t* b, int lane)
 
 /* Bounds, counts and channel orientation of the pixel subset `member`
    (bit i = pixel i); order-independent, so a lane can evaluate any subset. */
-__device__ inline AreaInfo AreaStats(const WarpState& st, const CellRegs& R, const Params& P, uint32_t member)
+__device__ inline NEBC7_SHARED AreaInfo AreaStats(const WarpState& st, const CellRegs& R, const Params& P, uint32_t member)
 {
 	AreaInfo a;
 	const uint32_t vis = member & R.visible;
@@ -624,7 +624,7 @@ __device__ inline AreaInfo AreaStats(const WarpState& st, const CellRegs& R, con
 /* Writes the ordered pixel list of a subset into `ar` (lanes 0..15).
    `anchor` is the subset's first pixel; members follow in ascending order,
    visible pixels first. */
-__device__ inline void BuildAreaList(Area& ar, const WarpState& st, const CellRegs& R, uint32_t member, int anchor, int lane)
+__device__ inline NEBC7_SHARED void BuildAreaList(Area& ar, const WarpState& st, const CellRegs& R, uint32_t member, int anchor, int lane)
 {
 	uint32_t rest = member & ~(1u << anchor);
 	/* position of every member in the selection order */

@@ -12,6 +12,14 @@
 
 namespace nebc7 {
 
+/* Marks the routines that many passes call (candidate lists, estimates,
+   combination searches, subset statistics): kept out of line so the kernel
+   holds one copy of each and its working set fits the instruction cache. */
+#ifndef NEBC7_SHARED
+#define NEBC7_SHARED __noinline__
+#endif
+
+
 static __constant__ int c_interp2[4] = { 0, 21, 43, 64 };
 static __constant__ int c_interp3[8] = { 0, 9, 18, 27, 37, 46, 55, 64 };
 static __constant__ int c_interp4[16] = { 0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64 };

@@ -208,16 +208,34 @@ __device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, cons
 	__syncwarp();
 }
 
+/* Dynamic shared memory of one encode CTA: the per-warp block state and,
+   for the refining instantiation, the per-warp search state. */
+template<bool NORMAL>
+constexpr size_t EncodeSharedBytes()
+{
+	return kWarpsPerCta * (sizeof(WarpState) + (NORMAL ? sizeof(SearchState) : 0));
+}
+
+/* Code shapes of the refining kernel.  Compact: every routine inlined (the
+   fastest for the default preset, whose time goes to one refinement).
+   Outlined: the routines the full searches call from many places kept out
+   of line (NEBC7_SHARED) and registers bounded for 4 CTAs per SM (the
+   fastest for the precise preset, /slow and /data, whose time goes to the
+   full searches).  The translation unit of an instantiation chooses
+   NEBC7_SHARED to match. */
+constexpr int kShapeCompact = 0;
+constexpr int kShapeOutlined = 1;
+
 /* NORMAL selects the refinement / full-search passes; only that
    instantiation reserves the per-warp search state in shared memory. */
-template<int kD, bool NORMAL>
-__global__ void __launch_bounds__(kWarpsPerCta * 32) KEncode(Job job, LevelTables T, Params P)
+template<int kD, bool NORMAL, int SHAPE>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4 : 1) KEncode(Job job, LevelTables T, Params P)
 {
-	__shared__ WarpState states[kWarpsPerCta];
-	__shared__ __align__(16) unsigned char searchRaw[NORMAL ? kWarpsPerCta * sizeof(SearchState) : 16];
+	extern __shared__ __align__(16) unsigned char encodeSmem[];
 	const int lane = threadIdx.x & 31;
-	WarpState& st = states[threadIdx.x >> 5];
-	SearchState* ss = NORMAL ? reinterpret_cast<SearchState*>(searchRaw) + (threadIdx.x >> 5) : nullptr;
+	const int warp = threadIdx.x >> 5;
+	WarpState& st = reinterpret_cast<WarpState*>(encodeSmem)[warp];
+	SearchState* ss = NORMAL ? reinterpret_cast<SearchState*>(encodeSmem + kWarpsPerCta * sizeof(WarpState)) + warp : nullptr;
 	for (;;)
 	{
 		int k = 0;
@@ -231,12 +249,12 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32) KEncode(Job job, LevelTable
 }
 
 /* Host-side launchers of KEncode.  Each instantiation is compiled in a
-   translation unit of its own (encode_d<kD>_<passes>.cu), so the four build
-   in parallel; the C ABI layer only sees these declarations. */
-template<int kD, bool NORMAL>
+   translation unit of its own (encode_d<kD>_<passes>.cu), so they build in
+   parallel; the C ABI layer only sees these declarations. */
+template<int kD, bool NORMAL, int SHAPE>
 cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T, const Params& P);
 
-template<int kD, bool NORMAL>
+template<int kD, bool NORMAL, int SHAPE>
 cudaError_t EncodeKernelOccupancy(int* ctasPerSm);
 
 } // namespace nebc7

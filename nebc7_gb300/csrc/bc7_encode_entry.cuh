@@ -8,22 +8,35 @@
 
 namespace nebc7 {
 
-template<int kD, bool NORMAL>
+/* Lets the kernel use more than the default 48 KB of dynamic shared memory
+   (once per process and device; idempotent). */
+template<int kD, bool NORMAL, int SHAPE>
+cudaError_t PrepareEncodeKernel()
+{
+	return cudaFuncSetAttribute(KEncode<kD, NORMAL, SHAPE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		int(EncodeSharedBytes<NORMAL>()));
+}
+
+template<int kD, bool NORMAL, int SHAPE>
 cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T, const Params& P)
 {
-	KEncode<kD, NORMAL><<<grid, kWarpsPerCta * 32, 0, stream>>>(job, T, P);
+	KEncode<kD, NORMAL, SHAPE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<NORMAL>(), stream>>>(job, T, P);
 	return cudaGetLastError();
 }
 
-template<int kD, bool NORMAL>
+template<int kD, bool NORMAL, int SHAPE>
 cudaError_t EncodeKernelOccupancy(int* ctasPerSm)
 {
-	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSm, KEncode<kD, NORMAL>, kWarpsPerCta * 32, 0);
+	const cudaError_t e = PrepareEncodeKernel<kD, NORMAL, SHAPE>();
+	if (e != cudaSuccess)
+		return e;
+	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSm, KEncode<kD, NORMAL, SHAPE>, kWarpsPerCta * 32,
+		EncodeSharedBytes<NORMAL>());
 }
 
 } // namespace nebc7
 
-#define NEBC7_INSTANTIATE_ENCODE(KD, NORMAL) \
-	template cudaError_t nebc7::LaunchEncodeKernel<KD, NORMAL>(int, cudaStream_t, const nebc7::Job&, \
+#define NEBC7_INSTANTIATE_ENCODE(KD, NORMAL, SHAPE) \
+	template cudaError_t nebc7::LaunchEncodeKernel<KD, NORMAL, SHAPE>(int, cudaStream_t, const nebc7::Job&, \
 		const nebc7::LevelTables&, const nebc7::Params&); \
-	template cudaError_t nebc7::EncodeKernelOccupancy<KD, NORMAL>(int*);
+	template cudaError_t nebc7::EncodeKernelOccupancy<KD, NORMAL, SHAPE>(int*);

@@ -138,8 +138,8 @@ __device__ __forceinline__ ChanList ZeroList(int2* nodes, int color, int lane)
 
 /* LevelsBuffer and LevelsBufferHalf: writes up to maxSize nodes (err, color). */
 template<int kD, bool HALF>
-__device__ ChanList ChannelLevels(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
-	int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int lane)
+__device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight,
+	int water, int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
 	const int shift = bits + int(pbits >= 0 || HALF);
@@ -258,10 +258,19 @@ __device__ ChanList ChannelLevels(int2* nodes, const Area& ar, const AreaInfo& a
 	return res;
 }
 
+/* Out-of-line copy of the scan for its many call sites; the Mode6Index2
+   refinement (the common case of the default preset) inlines the scan. */
+template<int kD, bool HALF>
+__device__ NEBC7_SHARED ChanList ChannelLevels(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
+	int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int lane)
+{
+	return ChannelLevelsScan<kD, HALF>(nodes, ar, ai, offset, weight, water, bits, pbits, transparent, table, maxSize, lane);
+}
+
 /* Single best candidate over the narrower window of the alpha slot of modes
    4 and 5 (src/SnippetLevelsBuffer.h:148-188, 433-490). */
 template<int kD>
-__device__ ChanList ChannelLevelsSingle(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
+__device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
 	int bits, bool transparent, const uint8_t* table, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
@@ -331,7 +340,7 @@ __device__ ChanList ChannelLevelsSingle(int2* nodes, const Area& ar, const AreaI
    lower bound.  The minimum does not depend on the visiting order, so rows
    are visited in order with the running best. */
 template<int kD>
-__device__ int EstimateChannelLevels(const Area& ar, const AreaInfo& ai, int offset, int weight, int water, int bits,
+__device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo& ai, int offset, int weight, int water, int bits,
 	bool transparent, const uint8_t* table, const uint16_t* tower, int lane)
 {
 	const int shift = bits;

@@ -26,13 +26,73 @@ namespace nebc7 {
 constexpr bool kHasNormalPasses = true;
 constexpr int kBig = 0x7FFFFFFF;
 
-struct SearchState
+struct __align__(16) SearchState
 {
 	int2 lists[4][4][32];    /* [p-bit variant][channel][entry] = (error, color) */
+	int planes[3][256];      /* partial error planes of the combination search, [pixel][level] */
 	int2 order[64];          /* full searches: (estimate, partition) */
-	int est[64][3][4];       /* per partition, subset, channel estimates */
-	int lines[64][3];
+	int est[64][3][3];       /* per partition, subset, channel (G, R, B) estimates */
+	int lines[64][2];        /* per partition, estimates of subsets 2 and 3 */
 };
+
+/* ---------------------------------------------------------------------- */
+/* Partial error planes                                                   */
+/*                                                                        */
+/* For endpoints fixed on some channels, plane[i][k] holds the weighted   */
+/* squared distances of pixel i to level k summed over those channels.    */
+/* A candidate for one more channel then costs one channel per pixel and  */
+/* level instead of all four; the sums are the same integers.             */
+/* ---------------------------------------------------------------------- */
+
+/* dst[i][k] = src[i][k] (0 without src) + w * q(x_i,c - v_k(col))^2 for the
+   first np pixels of the area, L = 1 << IB levels. */
+template<int kD, int IB>
+__device__ __forceinline__ void PlaneAdd(int* dst, const int* src, const Area& ar, int np, int c, int col, int w, int lane)
+{
+	constexpr int L = 1 << IB;
+	const int* wk = InterpWeights(IB);
+	const int e0 = col & 0xFF, e1 = (col >> 8) & 0xFF;
+	for (int e = lane; e < np * L; e += 32)
+	{
+		const int i = e >> IB, k = e & (L - 1);
+		const int q = Q<kD>(int(ar.px[i][c]) - Interp(e0, e1, wk[k]));
+		dst[e] = (src ? src[e] : 0) + w * q * q;
+	}
+	__syncwarp();
+}
+
+/* sum_i min_k (plane[i][k] + w * q(x_i,c - v_k(col))^2), stopping once the
+   sum reaches `limit` (the same partial sums as the four-channel error). */
+template<int kD, int IB>
+__device__ __forceinline__ int PlaneError(const int* plane, const Area& ar, int np, int c, int col, int w, int limit)
+{
+	constexpr int L = 1 << IB;
+	const int* wk = InterpWeights(IB);
+	const int e0 = col & 0xFF, e1 = (col >> 8) & 0xFF;
+	int v[L];
+#pragma unroll
+	for (int k = 0; k < L; k++)
+		v[k] = Interp(e0, e1, wk[k]);
+	int sum = 0;
+	for (int i = 0; i < np; i++)
+	{
+		const int x = ar.px[i][c];
+		const int4* row = reinterpret_cast<const int4*>(plane + i * L);
+		int best = kBig;
+#pragma unroll
+		for (int k4 = 0; k4 < L / 4; k4++)
+		{
+			const int4 pv = row[k4];
+			const int q0 = Q<kD>(x - v[4 * k4]), q1 = Q<kD>(x - v[4 * k4 + 1]);
+			const int q2 = Q<kD>(x - v[4 * k4 + 2]), q3 = Q<kD>(x - v[4 * k4 + 3]);
+			best = min(best, min(min(pv.x + w * q0 * q0, pv.y + w * q1 * q1), min(pv.z + w * q2 * q2, pv.w + w * q3 * q3)));
+		}
+		sum += best;
+		if (!(limit > sum))
+			break;
+	}
+	return sum;
+}
 
 /* ---------------------------------------------------------------------- */
 /* Errors over an area, with early exit at `water` (only used to reject)   */
@@ -156,29 +216,31 @@ __device__ __forceinline__ int ReplayInner(bool valid, int brk, int skip, int er
 /* ---------------------------------------------------------------------- */
 
 template<int kD, int IB>
-__device__ int TryVariants3(const Area& ar, const AreaInfo& ai, const Params& P, const int2* L1, ChanList c1,
-	const int2* L2, ChanList c2, const int2* L3, ChanList c3, Ep& best, int water, int lane)
+__device__ NEBC7_SHARED int TryVariants3(const Area& ar, const AreaInfo& ai, const Params& P, const int2* L1, ChanList c1,
+	const int2* L2, ChanList c2, const int2* L3, ChanList c3, Ep& best, int water, int* planes, int lane)
 {
 	const int min1 = c1.minErr, min2 = c2.minErr, min3 = c3.minErr;
 	if (min1 + min2 + min3 >= water)
 		return water;
-	const int wGR[4] = { 0, P.wG, P.wR, 0 };
-	const int wGB[4] = { 0, P.wG, 0, P.wB };
-	const int wGRB[4] = { 0, P.wG, P.wR, P.wB };
-	const int n2 = c2.count, n3 = c3.count;
+	const int n2 = c2.count, n3 = c3.count, np = ai.active;
+	int* pG = planes;
+	int* pGR = planes + 256;
+	const int col2l = lane < n2 ? L2[lane].y : 0;
+	const int col3 = lane < n3 ? L3[lane].y : 0;
+	const int e3base = lane < n3 ? L3[lane].x : kBig;
 	for (int i1 = 0; i1 < c1.count; i1++)
 	{
 		const int e1 = L1[i1].x;
 		if (e1 + min2 + min3 >= water)
 			break;
 		const int col1 = L1[i1].y;
+		/* memoised G+B errors (memGB) and G+R pair errors, one list entry per lane */
+		PlaneAdd<kD, IB>(pG, nullptr, ar, np, 1, col1, P.wG, lane);
 		int memGB = kBig, pairGR = kBig;
 		if (lane < n3)
-			memGB = AreaError<kD, IB>(ar, ai.active, Ep2(1, col1, 3, L3[lane].y), wGB, water - min2);
+			memGB = PlaneError<kD, IB>(pG, ar, np, 3, col3, P.wB, water - min2);
 		if (lane < n2)
-			pairGR = AreaError<kD, IB>(ar, ai.active, Ep2(1, col1, 2, L2[lane].y), wGR, water - min3);
-		const int col3 = lane < n3 ? L3[lane].y : 0;
-		const int e3base = lane < n3 ? L3[lane].x : kBig;
+			pairGR = PlaneError<kD, IB>(pG, ar, np, 2, col2l, P.wR, water - min3);
 		for (int i2 = 0; i2 < n2; i2++)
 		{
 			const int e2s = L2[i2].x + e1;
@@ -188,15 +250,13 @@ __device__ int TryVariants3(const Area& ar, const AreaInfo& ai, const Params& P,
 			const int e2 = __shfl_sync(kFull, pairGR, i2);
 			if (e2 + min3 >= water)
 				continue;
+			PlaneAdd<kD, IB>(pGR, pG, ar, np, 2, col2, P.wR, lane);
 			const bool valid = lane < n3;
 			const int brk = valid ? e3base + e2 : kBig;
 			const int skip = valid ? memGB + min2 : kBig;
 			int err = kBig;
 			if (valid && brk < water && skip < water)
-			{
-				const Ep ep = EpSetCh(Ep2(1, col1, 2, col2), 3, col3);
-				err = AreaError<kD, IB>(ar, ai.active, ep, wGRB, water);
-			}
+				err = PlaneError<kD, IB>(pGR, ar, np, 3, col3, P.wB, water);
 			const int jl = ReplayInner(valid, brk, skip, err, water, lane);
 			if (jl >= 0)
 				best = EpSetCh(Ep2(1, col1, 2, col2), 3, __shfl_sync(kFull, col3, jl));
@@ -274,7 +334,7 @@ __device__ int SearchSubset3(SearchState& ss, const Area& ar, const AreaInfo& ai
 	for (int v = 0; v < NumVariants3<MODE>(); v++)
 		if (valid[v])
 			water = TryVariants3<kD, IB>(ar, ai, P, ss.lists[v][0], cl[v][0], ss.lists[v][1], cl[v][1], ss.lists[v][2], cl[v][2],
-				best, water, lane);
+				best, water, &ss.planes[0][0], lane);
 	return water;
 }
 
@@ -420,11 +480,11 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
 				{
 					if (lane == 0)
 					{
-						ss.lines[p][1] = line2;
-						ss.lines[p][2] = line3;
+						ss.lines[p][0] = line2;
+						ss.lines[p][1] = line3;
 						for (int s = 0; s < 3; s++)
 							for (int c = 1; c < 4; c++)
-								ss.est[p][s][c] = e[s][c];
+								ss.est[p][s][c - 1] = e[s][c];
 						ss.order[count] = make_int2(R.opaqueAlphaError + line1 + line2 + line3 + step, p);
 					}
 					count++;
@@ -443,10 +503,10 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
 		{
 			const int p = o.y;
 			Ep mc[3] = { 0, 0, 0 };
-			const int line3 = ss.lines[p][2];
-			int e1[3] = { ss.est[p][0][1], ss.est[p][0][2], ss.est[p][0][3] };
+			const int line3 = ss.lines[p][1];
+			int e1[3] = { ss.est[p][0][0], ss.est[p][0][1], ss.est[p][0][2] };
 			const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 0, lane);
-			const int water1 = R.errTotal - step - R.opaqueAlphaError - ss.lines[p][1] - line3;
+			const int water1 = R.errTotal - step - R.opaqueAlphaError - ss.lines[p][0] - line3;
 			bool any;
 			int error = SearchSubset3<kD, MODE>(ss, st.sub[0], a1, P, T, water1, e1, mc[0], any, lane);
 			if (!any)
@@ -454,7 +514,7 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
 			if (error < water1)
 			{
 				error += R.opaqueAlphaError;
-				int e2[3] = { ss.est[p][1][1], ss.est[p][1][2], ss.est[p][1][3] };
+				int e2[3] = { ss.est[p][1][0], ss.est[p][1][1], ss.est[p][1][2] };
 				const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 1, lane);
 				const int water2 = R.errTotal - step - error - line3;
 				const int r2 = SearchSubset3<kD, MODE>(ss, st.sub[0], a2, P, T, water2, e2, mc[1], any, lane);
@@ -463,7 +523,7 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
 				error += r2;
 				if (error < R.errTotal - step - line3)
 				{
-					int e3[3] = { ss.est[p][2][1], ss.est[p][2][2], ss.est[p][2][3] };
+					int e3[3] = { ss.est[p][2][0], ss.est[p][2][1], ss.est[p][2][2] };
 					const AreaInfo a3 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 2, lane);
 					const int water3 = R.errTotal - step - error;
 					const int r3 = SearchSubset3<kD, MODE>(ss, st.sub[0], a3, P, T, water3, e3, mc[2], any, lane);
@@ -553,25 +613,26 @@ __device__ void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, cons
 /* ---------------------------------------------------------------------- */
 
 template<int kD, int IB, bool T4>
-__device__ int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, const int2* const* Ls,
-	const ChanList* cl, Ep& best, int water, int lane)
+__device__ __forceinline__ int TryVariants4Body(const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
+	const int2* const* Ls, const ChanList* cl, Ep& best, int water, int* planes, int lane)
 {
 	const int min0 = cl[0].minErr, min1 = cl[1].minErr, min2 = cl[2].minErr, min3 = cl[3].minErr;
 	if (min0 + min1 + min2 + min3 >= water)
 		return water;
-	const int n1 = cl[1].count, n2 = cl[2].count, n3 = cl[3].count;
+	const int n1 = cl[1].count, n2 = cl[2].count, n3 = cl[3].count, np = ai.active;
 	const bool opq = ai.opaque;
-	const int wAG[4] = { P.wA, P.wG, 0, 0 };
-	const int wAR[4] = { P.wA, 0, P.wR, 0 };
-	const int wGR[4] = { 0, P.wG, P.wR, 0 };
-	const int wAGR[4] = { P.wA, P.wG, P.wR, 0 };
-	const int wGB[4] = { 0, P.wG, 0, P.wB };
-	const int wAGB[4] = { P.wA, P.wG, 0, P.wB };
-	const int wAGRB[4] = { P.wA, P.wG, P.wR, P.wB };
 	const int2* L0 = Ls[0];
 	const int2* L1 = Ls[1];
 	const int2* L2 = Ls[2];
 	const int2* L3 = Ls[3];
+	/* an opaque area has alpha 255 and the alpha list holds 0xFFFF only, so the
+	   alpha plane is zero and the A-less weights of the reference's opaque
+	   branch give the same sums as the planes below */
+	int* pA = planes;
+	int* pAG = planes + 256;
+	int* pAGR = planes + 512;
+	const int col1l = lane < n1 ? L1[lane].y : 0;
+	const int col2l = lane < n2 ? L2[lane].y : 0;
 	const int col3 = lane < n3 ? L3[lane].y : 0;
 	const int e3base = lane < n3 ? L3[lane].x : kBig;
 	for (int i0 = 0; i0 < cl[0].count; i0++)
@@ -581,13 +642,14 @@ __device__ int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P,
 			break;
 		const int c0 = L0[i0].y;
 		const int ea = T4 ? TransparentError4(T, P, ai.count, ai.active, c0) : TransparentError2(T, P, ai.count, ai.active, c0);
+		PlaneAdd<kD, IB>(pA, nullptr, ar, np, 0, c0, P.wA, lane);
 		int memAR = kBig, pairAG = kBig;
 		if (!opq)
 		{
 			if (lane < n2)
-				memAR = AreaError<kD, IB>(ar, ai.active, Ep2(0, c0, 2, L2[lane].y), wAR, water - ea - min1 - min3) + ea;
+				memAR = PlaneError<kD, IB>(pA, ar, np, 2, col2l, P.wR, water - ea - min1 - min3) + ea;
 			if (lane < n1)
-				pairAG = AreaError<kD, IB>(ar, ai.active, Ep2(0, c0, 1, L1[lane].y), wAG, water - ea - min2 - min3) + ea;
+				pairAG = PlaneError<kD, IB>(pA, ar, np, 1, col1l, P.wG, water - ea - min2 - min3) + ea;
 		}
 		for (int i1 = 0; i1 < n1; i1++)
 		{
@@ -601,12 +663,13 @@ __device__ int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P,
 				if (e1 + min2 + min3 >= water)
 					continue;
 			}
+			PlaneAdd<kD, IB>(pAG, pA, ar, np, 1, c1, P.wG, lane);
 			int memAGB = kBig, pairAGR = kBig;
 			const Ep base01 = Ep2(0, c0, 1, c1);
 			if (lane < n3)
-				memAGB = AreaError<kD, IB>(ar, ai.active, EpSetCh(base01, 3, L3[lane].y), opq ? wGB : wAGB, water - ea - min2) + ea;
+				memAGB = PlaneError<kD, IB>(pAG, ar, np, 3, col3, P.wB, water - ea - min2) + ea;
 			if (lane < n2)
-				pairAGR = AreaError<kD, IB>(ar, ai.active, EpSetCh(base01, 2, L2[lane].y), opq ? wGR : wAGR, water - ea - min3) + ea;
+				pairAGR = PlaneError<kD, IB>(pAG, ar, np, 2, col2l, P.wR, water - ea - min3) + ea;
 			for (int i2 = 0; i2 < n2; i2++)
 			{
 				const int e2s = L2[i2].x + e1;
@@ -622,13 +685,14 @@ __device__ int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P,
 				const int e2 = __shfl_sync(kFull, pairAGR, i2);
 				if (e2 + min3 >= water)
 					continue;
+				PlaneAdd<kD, IB>(pAGR, pAG, ar, np, 2, c2, P.wR, lane);
 				const Ep base012 = EpSetCh(base01, 2, c2);
 				const bool valid = lane < n3;
 				const int brk = valid ? e3base + e2 : kBig;
 				const int skip = valid ? memAGB + min2 : kBig;
 				int err = kBig;
 				if (valid && brk < water && skip < water)
-					err = AreaError<kD, IB>(ar, ai.active, EpSetCh(base012, 3, col3), wAGRB, water - ea) + ea;
+					err = PlaneError<kD, IB>(pAGR, ar, np, 3, col3, P.wB, water - ea) + ea;
 				const int jl = ReplayInner(valid, brk, skip, err, water, lane);
 				if (jl >= 0)
 					best = EpSetCh(base012, 3, __shfl_sync(kFull, col3, jl));
@@ -636,6 +700,15 @@ __device__ int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P,
 		}
 	}
 	return water;
+}
+
+/* Out-of-line copy for modes 6 and 7; the Mode6Index2 refinement (the
+   common case of the default preset) inlines the body. */
+template<int kD, int IB, bool T4>
+__device__ NEBC7_SHARED int TryVariants4(const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, const int2* const* Ls,
+	const ChanList* cl, Ep& best, int water, int* planes, int lane)
+{
+	return TryVariants4Body<kD, IB, T4>(ar, ai, P, T, Ls, cl, best, water, planes, lane);
 }
 
 /* Subset::InitLevels of modes 6 / 6Index2 / 7 (src/Bc7CoreMode6.cpp:1130-1161,
@@ -661,7 +734,7 @@ __device__ bool InitLevels4(SearchState& ss, int v, int pbits, const Area& ar, c
 		}
 		else if (MODE == 9)
 		{
-			cl[c] = ChannelLevels<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, 20, lane);
+			cl[c] = ChannelLevelsScan<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, 20, lane);
 		}
 		else
 		{
@@ -680,8 +753,10 @@ __device__ int TryV4(SearchState& ss, int v, const Area& ar, const AreaInfo& ai,
 {
 	const int2* Ls[4] = { ss.lists[v][0], ss.lists[v][1], ss.lists[v][2], ss.lists[v][3] };
 	if (MODE == 6)
-		return TryVariants4<kD, 4, true>(ar, ai, P, T, Ls, cl, best, water, lane);
-	return TryVariants4<kD, 2, false>(ar, ai, P, T, Ls, cl, best, water, lane);
+		return TryVariants4<kD, 4, true>(ar, ai, P, T, Ls, cl, best, water, &ss.planes[0][0], lane);
+	if (MODE == 9)
+		return TryVariants4Body<kD, 2, false>(ar, ai, P, T, Ls, cl, best, water, &ss.planes[0][0], lane);
+	return TryVariants4<kD, 2, false>(ar, ai, P, T, Ls, cl, best, water, &ss.planes[0][0], lane);
 }
 
 /* Mode 6 / 6Index2 CompressSubset (src/Bc7CoreMode6.cpp:1334-1364): each
@@ -880,7 +955,7 @@ __device__ void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Par
 /* ---------------------------------------------------------------------- */
 
 template<int kD, int MODE, int CB, int AB>
-__device__ int TryVariantsRot(const Area& ar, const AreaInfo& ai, const Params& P, const int2* const* Ls, const ChanList* cl,
+__device__ NEBC7_SHARED int TryVariantsRot(const Area& ar, const AreaInfo& ai, const Params& P, const int2* const* Ls, const ChanList* cl,
 	Ep& bestStorage, int water, int rot, int lane)
 {
 	const int minA = cl[0].minErr, minG = cl[1].minErr, minR = cl[2].minErr, minB = cl[3].minErr;

@@ -1,4 +1,5 @@
-/* KEncode instantiation: exact differences (kDenoise 0), draft, refinement and full-search passes. */
+/* KEncode instantiation: exact differences (kDenoise 0), draft, refinement and full-search passes;
+   outlined shape (the precise preset runs the full searches on most blocks). */
 #include "bc7_encode_entry.cuh"
 
-NEBC7_INSTANTIATE_ENCODE(0, true)
+NEBC7_INSTANTIATE_ENCODE(0, true, nebc7::kShapeOutlined)

@@ -58,7 +58,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 	DeviceTables& D = gTables[dev][denoise];
 	if (!D.built)
 	{
-		const size_t sizes[14] = {
+		const size_t sizes[23] = {
 			size_t(256) * 65536, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
 			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
@@ -155,49 +155,73 @@ int ValidateSettings(const nebc7_settings* s)
 	return NEBC7_OK;
 }
 
-/* The four encode instantiations: denoise shift x refinement passes. */
+/* The encode instantiations: denoise shift x passes x code shape. */
 struct EncodeVariant
 {
 	cudaError_t (*launch)(int, cudaStream_t, const Job&, const LevelTables&, const Params&);
 	cudaError_t (*occupancy)(int*);
 };
 
-const EncodeVariant kVariants[4] = {
-	{ LaunchEncodeKernel<0, false>, EncodeKernelOccupancy<0, false> },
-	{ LaunchEncodeKernel<0, true>, EncodeKernelOccupancy<0, true> },
-	{ LaunchEncodeKernel<1, false>, EncodeKernelOccupancy<1, false> },
-	{ LaunchEncodeKernel<1, true>, EncodeKernelOccupancy<1, true> },
+constexpr int kNumVariants = 5;
+const EncodeVariant kVariants[kNumVariants] = {
+	{ LaunchEncodeKernel<0, false, kShapeCompact>, EncodeKernelOccupancy<0, false, kShapeCompact> },
+	{ LaunchEncodeKernel<0, true, kShapeOutlined>, EncodeKernelOccupancy<0, true, kShapeOutlined> },
+	{ LaunchEncodeKernel<1, false, kShapeCompact>, EncodeKernelOccupancy<1, false, kShapeCompact> },
+	{ LaunchEncodeKernel<1, true, kShapeCompact>, EncodeKernelOccupancy<1, true, kShapeCompact> },
+	{ LaunchEncodeKernel<1, true, kShapeOutlined>, EncodeKernelOccupancy<1, true, kShapeOutlined> },
 };
 
-int VariantSlot(int denoise, bool normal) { return (denoise ? 2 : 0) + (normal ? 1 : 0); }
-
-/* Resident CTAs per SM of one encode instantiation (cached per process;
-   every device of a process is the same GB300 part). */
-int CtasPerSm(int denoise, bool normal)
+/* Picks the instantiation: the compact shape for the stepped default preset
+   (kDenoise 1, refinement without /slow or /data), the outlined one where
+   the full searches dominate (measured on the 1024x1024 and 2048x2048
+   workloads). */
+int VariantSlot(const nebc7_settings& s)
 {
-	static int cache[4] = { 0, 0, 0, 0 };
-	const int slot = VariantSlot(denoise, normal);
-	if (!cache[slot])
-	{
-		int perSm = 0;
-		kVariants[slot].occupancy(&perSm);
-		cache[slot] = perSm > 0 ? perSm : 1;
-	}
-	return cache[slot];
+	if (!s.doNormal)
+		return s.denoise ? 2 : 0;
+	if (!s.denoise)
+		return 1;
+	return (s.doSlow || s.linearData) ? 4 : 3;
 }
 
-int GridFor(int nblocks, int denoise, bool normal)
+/* Launch shape of one encode instantiation on one device, looked up once
+   (with the device current): this also raises the kernel's dynamic
+   shared-memory limit, so it runs before the first launch on the device. */
+struct LaunchShape
 {
-	static int sms = 0;
-	if (!sms)
+	int sms = 0;
+	int perSm[kNumVariants] = {};
+};
+
+std::mutex gShapeMutex;
+LaunchShape gShapes[kMaxDevices];
+
+int GridFor(int nblocks, const nebc7_settings& s)
+{
+	int dev = 0;
+	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+		return 0;
+	const int slot = VariantSlot(s);
+	int sms, perSm;
 	{
-		int dev = 0;
-		cudaGetDevice(&dev);
-		cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-		if (sms <= 0)
-			sms = 1;
+		std::lock_guard<std::mutex> lock(gShapeMutex);
+		LaunchShape& L = gShapes[dev];
+		if (!L.sms)
+		{
+			cudaDeviceGetAttribute(&L.sms, cudaDevAttrMultiProcessorCount, dev);
+			if (L.sms <= 0)
+				L.sms = 1;
+		}
+		if (!L.perSm[slot])
+		{
+			int n = 0;
+			if (kVariants[slot].occupancy(&n) != cudaSuccess)
+				return 0;
+			L.perSm[slot] = n > 0 ? n : 1;
+		}
+		sms = L.sms;
+		perSm = L.perSm[slot];
 	}
-	const int perSm = CtasPerSm(denoise, normal);
 	const int ctasNeeded = (nblocks + kWarpsPerCta - 1) / kWarpsPerCta;
 	const int g = sms * perSm;
 	return ctasNeeded < g ? ctasNeeded : g;
@@ -252,9 +276,14 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 	job.counter = counter;
 	job.status = status;
 	const Params P = MakeParams(s);
-	const bool normal = s.doNormal != 0;
-	const int grid = GridFor(nblocks, s.denoise, normal);
-	CK(kVariants[VariantSlot(s.denoise, normal)].launch(grid, stream, job, *T, P));
+	const int grid = GridFor(nblocks, s);
+	if (grid <= 0)
+	{
+		if (!scratchIn)
+			cudaFreeAsync(scratch, stream);
+		return SetError(NEBC7_ECUDA);
+	}
+	CK(kVariants[VariantSlot(s)].launch(grid, stream, job, *T, P));
 
 	int rc = NEBC7_OK;
 	if (wantSums)
@@ -492,6 +521,10 @@ int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uin
 	if (int e = NoAllocScratch(dev, &scratch))
 		return e;
 
+	const int grid = GridFor(int(nb), *settings);
+	if (grid <= 0)
+		return SetError(NEBC7_ECUDA);
+
 	const cudaStream_t st = (cudaStream_t)stream;
 	/* the queue head and status word must start at zero */
 	CK(cudaMemsetAsync(scratch, 0, 256, st));
@@ -506,8 +539,7 @@ int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uin
 	job.counter = (int*)scratch;
 	job.status = (int*)scratch + 1;
 	const Params P = MakeParams(*settings);
-	const bool normal = settings->doNormal != 0;
-	CK(kVariants[VariantSlot(settings->denoise, normal)].launch(GridFor(int(nb), settings->denoise, normal), st, job, *T, P));
+	CK(kVariants[VariantSlot(*settings)].launch(grid, st, job, *T, P));
 	if (d_sums)
 	{
 		KReduceResults<<<1, 256, 0, st>>>(job.results, int(nb), (long long*)d_sums, (double*)((uint8_t*)d_sums + 16));
@@ -724,7 +756,8 @@ int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)
 	int dev = 0, sms = 0, perSm = 0;
 	CK(cudaGetDevice(&dev));
 	CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-	CK(kVariants[VariantSlot(1, true)].occupancy(&perSm));
+	const nebc7_settings def = { 1, 9, 1, 1, 0, 0 };
+	CK(kVariants[VariantSlot(def)].occupancy(&perSm));
 	if (ctas_per_sm)
 		*ctas_per_sm = perSm;
 	if (warps_per_cta)
