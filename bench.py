@@ -162,10 +162,50 @@ def cpu_rate(padded, mask, o, d, s, budget_s=12.0, threads=None):
     return done_px / spent / 1e6, threads, f"{done_px // pw} of {ph} pixel rows ({done_px} px), {spent:.1f} s", time.time() - t0
 
 
+def run_reference_batch(args, world):
+    """CPU arm of the batch: the oracle port over the batch's textures in
+    order, each step a bounded sample."""
+    from oracle.pyoracle import Port
+    port = Port()
+    inputs = batch_inputs(512, 4)
+    threads = os.cpu_count() or 1
+    rates = []
+    i = 0
+    for step in range(args.warmup + args.steps):
+        spent, done = 0.0, 0
+        while spent < args.cpu_budget / max(1, args.steps):
+            img, mask, preset = inputs[i % len(inputs)]
+            i += 1
+            d, s_, dr, no, sl, li = BATCH_PRESETS[preset]
+            port.lib.nebc7_oracle_init(d)
+            h, w = img.shape[:2]
+            out = np.zeros(((h // 4) * (w // 4), 16), np.uint8)
+            m = mask if mask is not None else np.full_like(img, 255)
+            t0 = time.time()
+            port.compress_texture(out, img, m, d, s_, dr, no, sl, li, threads=threads)
+            spent += time.time() - t0
+            done += h * w
+        if step >= args.warmup:
+            rates.append(done / spent / 1e6)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": "bc7_encode_Mpx_per_s", "value": value, "unit": "Mpx/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+        "config": {"workload": "batch512"},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port",
+                         "sample": "textures of the batch in order, bounded per step"},
+        "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     """CPU baseline arm: the oracle port on all host cores, rank 0 only."""
     if rank != 0:
         return
+    if args.workload == "batch512":
+        return run_reference_batch(args, world)
     padded, mask, o, d, s, gkey = prepare(args.workload)
     ph, pw = padded.shape[:2]
     rates = []
@@ -321,18 +361,157 @@ def run_ours(args, rank, world, local):
         dist.destroy_process_group()
 
 
+BATCH_PRESETS = {"draft": (1, 9, 1, 0, 0, 0), "default": (1, 9, 1, 1, 0, 0), "precise": (0, 0, 1, 1, 0, 0)}
+
+
+def batch_inputs(n, seed):
+    """The mixed batch: padded images, outline masks for the alpha ones."""
+    from nebc7_gb300 import synth
+    from nebc7_gb300.api import outline_mask, pad_texture
+    out = []
+    for d in synth.batch_textures(n, seed, 4, 2048):
+        img = pad_texture(synth.image_for(d["kind"], d["w"], d["h"], d["seed"]))
+        out.append((img, outline_mask(img, 1) if d["alpha"] else None, d["preset"]))
+    return out
+
+
+def run_batch(args, rank, world, local):
+    """512 textures of mixed sizes / presets as one plan (CUDA graph), against
+    per-image plain launches of the same textures on one stream."""
+    import torch
+    import nebc7_gb300
+    from nebc7_gb300 import Batch, BatchTexture
+    from nebc7_gb300._native import Settings
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nebc7_gb300.build()
+    lib = nebc7_gb300.load()
+    for d in (0, 1):
+        assert lib.nebc7_init_device(d) == 0
+    inputs = batch_inputs(512, 4)
+    px = sum(img.shape[0] * img.shape[1] for img, _, _ in inputs)
+    texs = []
+    for img, mask, preset in inputs:
+        h, w = img.shape[:2]
+        texs.append({"w": w, "h": h, "img": torch.from_numpy(img).to(dev),
+                     "mask": torch.from_numpy(mask).to(dev) if mask is not None else None,
+                     "dst": torch.zeros((h // 4) * (w // 4) * 16, dtype=torch.uint8, device=dev),
+                     "st": Settings(*BATCH_PRESETS[preset])})
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    # per-image plain launches (one stream, from scratch): reference outputs and time
+    plain_out = []
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for t in texs:
+        t["dst"].zero_()
+        rc = lib.nebc7_encode_device(t["dst"].data_ptr(), t["img"].data_ptr(),
+                                     t["mask"].data_ptr() if t["mask"] is not None else None, t["w"] * 4, t["w"], t["h"],
+                                     ctypes.byref(t["st"]), None, None, sp)
+        assert rc == 0
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_out = [t["dst"].clone() for t in texs]
+
+    b = Batch([BatchTexture(t["dst"].data_ptr(), t["img"].data_ptr(),
+                            t["mask"].data_ptr() if t["mask"] is not None else None, t["w"] * 4, t["w"], t["h"], t["st"])
+               for t in texs], from_scratch=True)
+    tune_ms = b.tune(1)
+    info = b.info()
+    for _ in range(args.warmup):
+        b.launch(sp)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with NvmlSampler(dev) as clocks:
+        for i in range(args.steps):
+            starts[i].record(stream)
+            b.launch(sp)
+            ends[i].record(stream)
+        torch.cuda.synchronize()
+    step_ms = sum(a.elapsed_time(c) for a, c in zip(starts, ends)) / args.steps
+    exact = all(torch.equal(t["dst"], o) for t, o in zip(texs, plain_out))
+
+    # end to end: pinned host inputs in, blocks out, every step
+    h_img = [t["img"].cpu().pin_memory() for t in texs]
+    h_mask = [t["mask"].cpu().pin_memory() if t["mask"] is not None else None for t in texs]
+    h_dst = [torch.empty_like(t["dst"], device="cpu").pin_memory() for t in texs]
+    e2e = []
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for t, hi, hm in zip(texs, h_img, h_mask):
+            t["img"].copy_(hi, non_blocking=True)
+            if hm is not None:
+                t["mask"].copy_(hm, non_blocking=True)
+        b.launch(sp)
+        for t, hd in zip(texs, h_dst):
+            hd.copy_(t["dst"], non_blocking=True)
+        torch.cuda.synchronize()
+        e2e.append(time.perf_counter() - t0)
+    e2e_s = float(np.mean(e2e[args.warmup:]))
+    h2d = sum(t["img"].numel() + (t["mask"].numel() if t["mask"] is not None else 0) for t in texs)
+    d2h = sum(t["dst"].numel() for t in texs)
+    b.close()
+
+    if rank == 0:
+        # CPU baseline: the oracle port on the host cores over the first textures, bounded
+        from oracle.pyoracle import Port
+        port = Port()
+        spent, done = 0.0, 0
+        for img, mask, preset in inputs:
+            if spent >= args.cpu_budget:
+                break
+            d, s_, dr, no, sl, li = BATCH_PRESETS[preset]
+            port.lib.nebc7_oracle_init(d)
+            h, w = img.shape[:2]
+            out = np.zeros(((h // 4) * (w // 4), 16), np.uint8)
+            m = mask if mask is not None else np.full_like(img, 255)
+            t0 = time.time()
+            port.compress_texture(out, img, m, d, s_, dr, no, sl, li, threads=os.cpu_count() or 1)
+            spent += time.time() - t0
+            done += h * w
+        line = {
+            "metric": "bc7_encode_Mpx_per_s", "value": px * world / (step_ms / 1e3) / 1e6, "unit": "Mpx/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "batch512", "textures": len(texs), "pixels": px,
+                       "sides": "log-uniform 4..2048 per axis, x4", "mix": "60% opaque / 40% alpha (outline mask); "
+                       "draft / default / precise", "l2": "inputs (%.0f MB) larger than L2" % (h2d / 1e6),
+                       "bit_exact_vs_plain_launches": bool(exact), "schedule": info["schedule"],
+                       "launches_per_step": info["launches"], "tune_ms": list(tune_ms),
+                       "parallelism": f"replicas{world}"},
+            "plain_per_image": {"value": px / (plain_ms / 1e3) / 1e6, "unit": "Mpx/s", "ms": plain_ms,
+                                "launches": len(texs)},
+            "e2e": {"value": px * world / e2e_s / 1e6, "unit": "Mpx/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * info["launches"],
+            "cpu_baseline": {"value": done / spent / 1e6 if spent else None, "unit": "Mpx/s",
+                             "cores": os.cpu_count(), "kind": "port",
+                             "sample": f"first textures of the batch, {done} px, {spent:.1f} s"},
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"], default=DEFAULT_WORKLOAD)
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the baseline sample")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload == "batch512":
+        run_batch(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -169,6 +169,55 @@ int nebc7_init_device(int denoise);
 int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uint8_t* d_mask, long long stride, int w,
 	int h, const nebc7_settings* settings, void* d_sums, void* stream);
 
+/* ---- batches (no counterpart in the reference) ------------------------- */
+
+/* One texture of a batch: device buffers as for nebc7_encode_device. */
+typedef struct nebc7_texture
+{
+	uint8_t* d_dst;            /* w*h/16 blocks, 16-byte aligned: starting blocks in, result out */
+	const uint8_t* d_bgra;     /* padded BGRA rows, `stride` bytes apart */
+	const uint8_t* d_mask;     /* mask rows (A,G,R,B bytes) or null */
+	long long stride;
+	int w, h;                  /* multiples of 4 */
+	nebc7_settings settings;   /* the texture's own preset and flags */
+} nebc7_texture;
+
+typedef struct nebc7_batch nebc7_batch;
+
+#define NEBC7_BATCH_FROM_SCRATCH 1   /* every launch clears the outputs first */
+
+/* Plans a batch of textures of any sizes and presets: one persistent
+   kernel launch over a global block queue (textures of the longest
+   expected work first), or one such launch per preset group on concurrent
+   streams.  Allocates the plan's device tables and scratch (per-block
+   results, per-texture sums) on the current device; the textures' buffers
+   stay the caller's and must outlive the plan. */
+int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_batch** out);
+
+/* Times both schedules `trials` times (as CUDA graphs) and keeps the faster
+   for nebc7_batch_launch; restores the starting blocks afterwards unless
+   the plan clears them itself.  ms_out[2], if non-null, receives the best
+   times of the mixed and the grouped schedule (3.4e38 if not tried). */
+int nebc7_batch_tune(nebc7_batch* b, int trials, float* ms_out);
+
+/* Enqueues the batch on `stream` by replaying its CUDA graph (captured on
+   the first call for the chosen schedule).  Outputs and sums are ready
+   when the stream reaches this point. */
+int nebc7_batch_launch(nebc7_batch* b, void* stream);
+
+/* Copies the per-texture sums of the last launch (errs[2 i] = Error.Alpha
+   << 2kD, errs[2 i + 1] = color part, ssim[2 i], ssim[2 i + 1]; either may
+   be null) after waiting for `stream`. */
+int nebc7_batch_sums(nebc7_batch* b, void* stream, int64_t* errs, double* ssim);
+
+/* Overrides the schedule: 0 one mixed launch, 1 one launch per preset group. */
+int nebc7_batch_set_schedule(nebc7_batch* b, int schedule);
+
+/* Chosen schedule (0 mixed, 1 grouped), kernel launches per run, blocks. */
+int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* blocks);
+
+void nebc7_batch_destroy(nebc7_batch* b);
+
 /* Persistent-grid sizing of the encode kernel of the default preset
    (kDenoise 1 with the refinement passes): CTAs per SM and warps per CTA. */
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);

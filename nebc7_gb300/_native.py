@@ -102,6 +102,22 @@ class BlockSSIM(ctypes.Structure):
     _fields_ = [("Alpha", ctypes.c_double), ("Color", ctypes.c_double)]
 
 
+class Texture(ctypes.Structure):
+    """nebc7_texture: one texture of a batch (device buffers)."""
+
+    _fields_ = [
+        ("d_dst", VP),
+        ("d_bgra", VP),
+        ("d_mask", VP),
+        ("stride", LL),
+        ("w", I),
+        ("h", I),
+        ("settings", Settings),
+    ]
+
+
+BATCH_FROM_SCRATCH = 1
+
 PInitTables = ctypes.CFUNCTYPE(None, ctypes.c_bool, ctypes.c_bool, ctypes.c_bool, ctypes.c_bool)
 PBlockKernel = ctypes.CFUNCTYPE(None, ctypes.POINTER(WorkerItem), ctypes.POINTER(WorkerItem), I,
                                 ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(BlockSSIM))
@@ -132,6 +148,13 @@ SIGNATURES = {
     "nebc7_init_device": (I, [I]),
     "nebc7_launch_shape": (I, [VP, VP, VP]),
     "nebc7_encode_device_noalloc": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),
+    "nebc7_batch_create": (I, [VP, I, I, VP]),
+    "nebc7_batch_tune": (I, [VP, I, VP]),
+    "nebc7_batch_launch": (I, [VP, VP]),
+    "nebc7_batch_sums": (I, [VP, VP, VP, VP]),
+    "nebc7_batch_set_schedule": (I, [VP, I]),
+    "nebc7_batch_info": (I, [VP, VP, VP, VP]),
+    "nebc7_batch_destroy": (None, [VP]),
 }
 
 

@@ -237,7 +237,83 @@ def encode_device(dst_ptr: int, bgra_ptr: int, mask_ptr: int | None, stride: int
     return None
 
 
+@dataclass
+class BatchTexture:
+    """One texture of a Batch: raw CUDA device pointers and its own preset."""
+
+    dst: int
+    bgra: int
+    mask: int | None
+    stride: int
+    width: int
+    height: int
+    settings: Settings
+
+
+class Batch:
+    """Many textures of any sizes and presets encoded by one plan: a
+    persistent launch over a global block queue (or one per preset group on
+    concurrent streams), replayed as a CUDA graph.  Device buffers stay the
+    caller's and must outlive the Batch."""
+
+    MIXED, GROUPED = 0, 1
+
+    def __init__(self, textures: list[BatchTexture], from_scratch: bool = False):
+        self._lib = _native.load()
+        arr = (_native.Texture * len(textures))()
+        for i, t in enumerate(textures):
+            arr[i].d_dst = t.dst
+            arr[i].d_bgra = t.bgra
+            arr[i].d_mask = t.mask
+            arr[i].stride = t.stride
+            arr[i].w = t.width
+            arr[i].h = t.height
+            arr[i].settings = t.settings
+        self._n = len(textures)
+        self._h = ctypes.c_void_p()
+        check(self._lib.nebc7_batch_create(ctypes.cast(arr, ctypes.c_void_p), self._n,
+                                           _native.BATCH_FROM_SCRATCH if from_scratch else 0,
+                                           ctypes.byref(self._h)), "batch_create")
+
+    def tune(self, trials: int = 2) -> tuple[float, float]:
+        """Times both schedules and keeps the faster; returns their best ms."""
+        ms = (ctypes.c_float * 2)()
+        check(self._lib.nebc7_batch_tune(self._h, trials, ctypes.cast(ms, ctypes.c_void_p)), "batch_tune")
+        return float(ms[0]), float(ms[1])
+
+    def set_schedule(self, which: int) -> None:
+        check(self._lib.nebc7_batch_set_schedule(self._h, which), "batch_set_schedule")
+
+    def launch(self, stream: int = 0) -> None:
+        check(self._lib.nebc7_batch_launch(self._h, stream), "batch_launch")
+
+    def sums(self, stream: int = 0) -> tuple[np.ndarray, np.ndarray]:
+        """Per-texture (errAlpha, errColor) and (ssimAlpha, ssimColor) of the last launch."""
+        errs = np.zeros((self._n, 2), np.int64)
+        ssim = np.zeros((self._n, 2), np.float64)
+        check(self._lib.nebc7_batch_sums(self._h, stream, _ptr(errs), _ptr(ssim)), "batch_sums")
+        return errs, ssim
+
+    def info(self) -> dict:
+        sched, launches, blocks = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.nebc7_batch_info(self._h, ctypes.byref(sched), ctypes.byref(launches),
+                                         ctypes.byref(blocks)), "batch_info")
+        return {"schedule": ("mixed", "grouped")[sched.value], "launches": launches.value, "blocks": blocks.value}
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.nebc7_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 __all__ = [
     "Bc7Core", "Preset", "DEFAULT", "PRECISE", "EncodeStats", "EncodedImage", "NativeError",
     "encode_image", "encode_device", "pad_texture", "outline_mask", "padded_size", "parse_flags",
+    "Batch", "BatchTexture",
 ]

@@ -68,4 +68,50 @@ __global__ void KReduceResults(const BlockResult* r, int n, long long* errs, dou
 	}
 }
 
+/* Per-texture sums of a batch: CTA t reduces the per-block results of
+   table entry t over its queue positions, with the same fixed tree as
+   KReduceResults (so a texture's sums do not depend on the batch), into
+   sums[tex[t].id] = { errAlpha, errColor } and ssims[...] = { alpha, color }. */
+__global__ void KReduceTextures(const BlockResult* r, const TexDesc* tex, long long* errs, double* ssims)
+{
+	__shared__ long long sa[256], sc[256];
+	__shared__ double qa[256], qc[256];
+	const TexDesc& d = tex[blockIdx.x];
+	const BlockResult* rr = r + d.first;
+	const int n = d.nblocks;
+	const int t = threadIdx.x;
+	long long a = 0, c = 0;
+	double x = 0, y = 0;
+	for (int i = t; i < n; i += 256)
+	{
+		a += rr[i].errAlpha;
+		c += rr[i].errColor;
+		x = __dadd_rn(x, rr[i].ssimAlpha);
+		y = __dadd_rn(y, rr[i].ssimColor);
+	}
+	sa[t] = a;
+	sc[t] = c;
+	qa[t] = x;
+	qc[t] = y;
+	__syncthreads();
+	for (int s = 128; s > 0; s >>= 1)
+	{
+		if (t < s)
+		{
+			sa[t] += sa[t + s];
+			sc[t] += sc[t + s];
+			qa[t] = __dadd_rn(qa[t], qa[t + s]);
+			qc[t] = __dadd_rn(qc[t], qc[t + s]);
+		}
+		__syncthreads();
+	}
+	if (t == 0)
+	{
+		errs[2 * d.id] = sa[0];
+		errs[2 * d.id + 1] = sc[0];
+		ssims[2 * d.id] = qa[0];
+		ssims[2 * d.id + 1] = qc[0];
+	}
+}
+
 } // namespace nebc7

@@ -24,8 +24,9 @@ struct BlockResult
 	double ssimAlpha, ssimColor;
 };
 
-/* Per-launch description of where the blocks are. */
-struct Job
+/* One texture of a launch: padded BGRA rows and optional mask rows, its
+   blocks in row-major order, and its preset. */
+struct TexDesc
 {
 	uint8_t* dst;            /* 16 bytes per block, read as the starting block */
 	const uint8_t* bgra;     /* top-left pixel of block 0 */
@@ -33,26 +34,51 @@ struct Job
 	long long stride;        /* bytes between pixel rows */
 	int blocksW;             /* blocks per block row */
 	int nblocks;
-	BlockResult* results;    /* optional, one per block */
+	int first;               /* queue position of its first block */
+	int denoise;             /* kDenoise of its preset */
+	int id;                  /* caller's index of the texture (batches) */
+	Params P;
+};
+
+/* Per-launch description: the textures and the shared work queue.  The
+   queue deals blocks in texture-table order; a warp finds the texture of a
+   queue position by binary search over `first`. */
+struct Job
+{
+	const TexDesc* tex;      /* device table of ntex textures, or null: `single` */
+	TexDesc single;
+	int ntex;
+	int total;               /* blocks over all textures */
+	BlockResult* results;    /* optional, one per queue position */
 	int* counter;            /* work queue head, zero before launch */
 	int* status;             /* set non-zero on an internal limit */
 };
 
+/* kD template value of the kernel that reads kDenoise from each texture */
+constexpr int kAnyDenoise = 2;
+
 constexpr int kWarpsPerCta = 4;
 
-template<int kD, bool NORMAL>
-__device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T, const Params& P, int k, int lane)
+/* Where one block's pixels, mask and 16 output bytes are. */
+struct BlockRef
 {
-	const int bx = k % job.blocksW, by = k / job.blocksW;
-	const long long base = (long long)by * 4 * job.stride + (long long)bx * 16;
+	const uint8_t* bgra;     /* top-left pixel of the block */
+	const uint8_t* mask;     /* same position in the mask, or null */
+	long long stride;        /* bytes between pixel rows */
+	uint8_t* out;            /* the block: starting block in, result out */
+	BlockResult* result;     /* optional */
+};
 
+template<int kD, bool NORMAL>
+__device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b, const LevelTables& T, const Params& P, int lane)
+{
 	/* coalesced load: lanes 0..15 read one BGRA pixel, 16..31 its mask */
 	{
 		const int i = lane & 15;
-		const long long off = base + (long long)(i >> 2) * job.stride + (i & 3) * 4;
+		const long long off = (long long)(i >> 2) * b.stride + (i & 3) * 4;
 		if (lane < 16)
 		{
-			const uchar4 p = *reinterpret_cast<const uchar4*>(job.bgra + off);
+			const uchar4 p = *reinterpret_cast<const uchar4*>(b.bgra + off);
 			st.img[i][0] = p.w;
 			st.img[i][1] = p.y;
 			st.img[i][2] = p.z;
@@ -61,15 +87,15 @@ __device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, cons
 		else
 		{
 			uchar4 m = make_uchar4(0xFF, 0xFF, 0xFF, 0xFF);
-			if (job.mask)
-				m = *reinterpret_cast<const uchar4*>(job.mask + off);
+			if (b.mask)
+				m = *reinterpret_cast<const uchar4*>(b.mask + off);
 			st.msk[i][0] = m.x;
 			st.msk[i][1] = m.y;
 			st.msk[i][2] = m.z;
 			st.msk[i][3] = m.w;
 		}
 	}
-	const uint4 blk = *reinterpret_cast<const uint4*>(job.dst + (long long)k * 16);
+	const uint4 blk = *reinterpret_cast<const uint4*>(b.out);
 	__syncwarp();
 
 	uint64_t lo = uint64_t(blk.x) | (uint64_t(blk.y) << 32);
@@ -169,7 +195,7 @@ __device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, cons
 				}
 			}
 
-			if (NORMAL)
+			if (NORMAL && P.doNormal)
 				NormalPasses<kD>(st, *ss, R, P, T, lane);
 
 			if (water > R.errTotal)
@@ -193,19 +219,58 @@ __device__ void EncodeBlock(WarpState& st, SearchState* ss, const Job& job, cons
 
 	if (lane == 0)
 	{
-		*reinterpret_cast<uint4*>(job.dst + (long long)k * 16) =
-			make_uint4(unsigned(lo), unsigned(lo >> 32), unsigned(hi), unsigned(hi >> 32));
-		if (job.results)
+		*reinterpret_cast<uint4*>(b.out) = make_uint4(unsigned(lo), unsigned(lo >> 32), unsigned(hi), unsigned(hi >> 32));
+		if (b.result)
 		{
 			BlockResult r;
 			r.errAlpha = int(unsigned(R.errAlpha) << (kD + kD));
 			r.errColor = int(unsigned(R.errTotal - R.errAlpha) << (kD + kD));
 			r.ssimAlpha = qa;
 			r.ssimColor = qc;
-			job.results[k] = r;
+			*b.result = r;
 		}
 	}
 	__syncwarp();
+}
+
+/* Encodes queue position k of the launch. */
+template<int kD, bool NORMAL>
+__device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T0,
+	const LevelTables& T1, int k, int lane)
+{
+	int t = 0;
+	if (job.tex)
+	{
+		int hi = job.ntex - 1;
+		while (t < hi)
+		{
+			const int mid = (t + hi + 1) >> 1;
+			if (job.tex[mid].first <= k)
+				t = mid;
+			else
+				hi = mid - 1;
+		}
+	}
+	const TexDesc& d = job.tex ? job.tex[t] : job.single;
+	const int local = k - d.first;
+	const int bx = local % d.blocksW, by = local / d.blocksW;
+	const long long base = (long long)by * 4 * d.stride + (long long)bx * 16;
+	BlockRef b;
+	b.bgra = d.bgra + base;
+	b.mask = d.mask ? d.mask + base : nullptr;
+	b.stride = d.stride;
+	b.out = d.dst + (long long)local * 16;
+	b.result = job.results ? job.results + k : nullptr;
+	const Params P = d.P;
+	if (kD == kAnyDenoise)
+	{
+		if (d.denoise)
+			EncodeBlockAt<1, NORMAL>(st, ss, b, T1, P, lane);
+		else
+			EncodeBlockAt<0, NORMAL>(st, ss, b, T0, P, lane);
+	}
+	else
+		EncodeBlockAt<kD == 1 ? 1 : 0, NORMAL>(st, ss, b, kD ? T1 : T0, P, lane);
 }
 
 /* Dynamic shared memory of one encode CTA: the per-warp block state and,
@@ -226,10 +291,13 @@ constexpr size_t EncodeSharedBytes()
 constexpr int kShapeCompact = 0;
 constexpr int kShapeOutlined = 1;
 
-/* NORMAL selects the refinement / full-search passes; only that
-   instantiation reserves the per-warp search state in shared memory. */
+/* Persistent encode kernel over a launch's textures.  NORMAL compiles the
+   refinement / full-search passes (run for textures whose preset asks for
+   them); only that instantiation reserves the per-warp search state in
+   shared memory.  kD: the kDenoise of every texture, or kAnyDenoise. */
 template<int kD, bool NORMAL, int SHAPE>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4 : 1) KEncode(Job job, LevelTables T, Params P)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4 : 1)
+	KEncode(Job job, LevelTables T0, LevelTables T1)
 {
 	extern __shared__ __align__(16) unsigned char encodeSmem[];
 	const int lane = threadIdx.x & 31;
@@ -242,9 +310,9 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4
 		if (lane == 0)
 			k = atomicAdd(job.counter, 1);
 		k = __shfl_sync(kFull, k, 0);
-		if (k >= job.nblocks)
+		if (k >= job.total)
 			break;
-		EncodeBlock<kD, NORMAL>(st, ss, job, T, P, k, lane);
+		EncodeQueued<kD, NORMAL>(st, ss, job, T0, T1, k, lane);
 	}
 }
 
@@ -252,7 +320,7 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4
    translation unit of its own (encode_d<kD>_<passes>.cu), so they build in
    parallel; the C ABI layer only sees these declarations. */
 template<int kD, bool NORMAL, int SHAPE>
-cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T, const Params& P);
+cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T0, const LevelTables& T1);
 
 template<int kD, bool NORMAL, int SHAPE>
 cudaError_t EncodeKernelOccupancy(int* ctasPerSm);

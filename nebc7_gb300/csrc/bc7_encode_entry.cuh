@@ -18,9 +18,9 @@ cudaError_t PrepareEncodeKernel()
 }
 
 template<int kD, bool NORMAL, int SHAPE>
-cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T, const Params& P)
+cudaError_t LaunchEncodeKernel(int grid, cudaStream_t stream, const Job& job, const LevelTables& T0, const LevelTables& T1)
 {
-	KEncode<kD, NORMAL, SHAPE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<NORMAL>(), stream>>>(job, T, P);
+	KEncode<kD, NORMAL, SHAPE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<NORMAL>(), stream>>>(job, T0, T1);
 	return cudaGetLastError();
 }
 
@@ -38,5 +38,5 @@ cudaError_t EncodeKernelOccupancy(int* ctasPerSm)
 
 #define NEBC7_INSTANTIATE_ENCODE(KD, NORMAL, SHAPE) \
 	template cudaError_t nebc7::LaunchEncodeKernel<KD, NORMAL, SHAPE>(int, cudaStream_t, const nebc7::Job&, \
-		const nebc7::LevelTables&, const nebc7::Params&); \
+		const nebc7::LevelTables&, const nebc7::LevelTables&); \
 	template cudaError_t nebc7::EncodeKernelOccupancy<KD, NORMAL, SHAPE>(int*);

@@ -189,29 +189,36 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	int stored = 0;
 	int zeros = 0;
 	const int rowStep = pvar ? 2 : 1;
-	for (int iH = win.HL + (pvar ? pH : 0); iH < win.HH; iH += rowStep)
+	/* hL - cH = LH for every row: when LH is below one chunk, only the first
+	   chunk of a row can be on and a batch takes two rows (lanes 16..31 the
+	   second); the candidate set and the kept keys are unchanged */
+	const int W = pvar ? 32 : 16;
+	const bool twoRows = win.LH < W;
+	for (int iH0 = win.HL + (pvar ? pH : 0); iH0 < win.HH; iH0 += twoRows ? 2 * rowStep : rowStep)
 	{
-		const int cH = iH << shift;
-		const int hL = win.LH + cH;
 		/* candidates in batches of 32: two 16-candidate chunks per batch */
 		for (int b = 0;; b++)
 		{
 			const int half = lane >> 4, j = lane & 15;
+			const int iH = twoRows ? iH0 + half * rowStep : iH0;
+			const int cH = iH << shift;
+			const int hL = win.LH + cH;
+			const int chunk = twoRows ? b : 2 * b + half;
 			int c, cc;
 			unsigned flags;
 			if (pvar)
 			{
-				c = cH + 64 * b + 32 * half;
+				c = cH + 32 * chunk;
 				cc = c + pL + 2 * j;
 				flags = Shr32(~0u, unsigned(max(0, Wsub(c | 31, hL | 7))));
 			}
 			else
 			{
-				c = cH + 32 * b + 16 * half;
+				c = cH + 16 * chunk;
 				cc = c + j;
 				flags = Shr32(~0u, unsigned(max(0, Wsub(c | 15, hL | 7))) << 1);
 			}
-			const bool chunkOn = (c == cH) || (c <= hL);
+			const bool chunkOn = (iH < win.HH) && ((c == cH) || (c <= hL));
 			const bool on = chunkOn && ((flags >> (2 * j)) & 1);
 			if (!__any_sync(kFull, chunkOn))
 				break;
@@ -294,17 +301,20 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 	const int rowSize = 1 << (2 * shift);
 
 	unsigned best = 0xFFFFFFFFu;
-	for (int iH = win.HL; iH < win.HH; iH++)
+	/* two rows per batch when only a row's first chunk can be on */
+	const bool twoRows = win.LH < 16;
+	for (int iH0 = win.HL; iH0 < win.HH; iH0 += twoRows ? 2 : 1)
 	{
-		const int cH = iH << shift;
-		const int hL = min(win.LH, iH) + cH;
 		for (int b = 0;; b++)
 		{
 			const int half = lane >> 4, j = lane & 15;
-			const int c = cH + 32 * b + 16 * half;
+			const int iH = twoRows ? iH0 + half : iH0;
+			const int cH = iH << shift;
+			const int hL = min(win.LH, iH) + cH;
+			const int c = cH + 16 * (twoRows ? b : 2 * b + half);
 			const int cc = c + j;
 			const unsigned mask = Shr32(~0u, unsigned(max(0, Wsub(c | 15, hL | 7))) << 1);
-			const bool chunkOn = (c == cH) || (c <= hL);
+			const bool chunkOn = (iH < win.HH) && ((c == cH) || (c <= hL));
 			if (!__any_sync(kFull, chunkOn))
 				break;
 			if (chunkOn && ((mask >> (2 * j)) & 1))

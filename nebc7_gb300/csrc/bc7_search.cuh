@@ -664,8 +664,8 @@ __device__ __forceinline__ int TryVariants4Body(const Area& ar, const AreaInfo& 
 					continue;
 			}
 			PlaneAdd<kD, IB>(pAG, pA, ar, np, 1, c1, P.wG, lane);
-			int memAGB = kBig, pairAGR = kBig;
 			const Ep base01 = Ep2(0, c0, 1, c1);
+			int memAGB = kBig, pairAGR = kBig;
 			if (lane < n3)
 				memAGB = PlaneError<kD, IB>(pAG, ar, np, 3, col3, P.wB, water - ea - min2) + ea;
 			if (lane < n2)

@@ -13,6 +13,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 #include <string.h>
 #include <vector>
@@ -158,17 +159,19 @@ int ValidateSettings(const nebc7_settings* s)
 /* The encode instantiations: denoise shift x passes x code shape. */
 struct EncodeVariant
 {
-	cudaError_t (*launch)(int, cudaStream_t, const Job&, const LevelTables&, const Params&);
+	cudaError_t (*launch)(int, cudaStream_t, const Job&, const LevelTables&, const LevelTables&);
 	cudaError_t (*occupancy)(int*);
 };
 
-constexpr int kNumVariants = 5;
+constexpr int kNumVariants = 6;
+constexpr int kVariantMixed = 5;   /* batches: kDenoise per texture */
 const EncodeVariant kVariants[kNumVariants] = {
 	{ LaunchEncodeKernel<0, false, kShapeCompact>, EncodeKernelOccupancy<0, false, kShapeCompact> },
 	{ LaunchEncodeKernel<0, true, kShapeOutlined>, EncodeKernelOccupancy<0, true, kShapeOutlined> },
 	{ LaunchEncodeKernel<1, false, kShapeCompact>, EncodeKernelOccupancy<1, false, kShapeCompact> },
 	{ LaunchEncodeKernel<1, true, kShapeCompact>, EncodeKernelOccupancy<1, true, kShapeCompact> },
 	{ LaunchEncodeKernel<1, true, kShapeOutlined>, EncodeKernelOccupancy<1, true, kShapeOutlined> },
+	{ LaunchEncodeKernel<kAnyDenoise, true, kShapeOutlined>, EncodeKernelOccupancy<kAnyDenoise, true, kShapeOutlined> },
 };
 
 /* Picks the instantiation: the compact shape for the stepped default preset
@@ -196,12 +199,11 @@ struct LaunchShape
 std::mutex gShapeMutex;
 LaunchShape gShapes[kMaxDevices];
 
-int GridFor(int nblocks, const nebc7_settings& s)
+int GridForSlot(int nblocks, int slot)
 {
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
 		return 0;
-	const int slot = VariantSlot(s);
 	int sms, perSm;
 	{
 		std::lock_guard<std::mutex> lock(gShapeMutex);
@@ -225,6 +227,34 @@ int GridFor(int nblocks, const nebc7_settings& s)
 	const int ctasNeeded = (nblocks + kWarpsPerCta - 1) / kWarpsPerCta;
 	const int g = sms * perSm;
 	return ctasNeeded < g ? ctasNeeded : g;
+}
+
+int GridFor(int nblocks, const nebc7_settings& s)
+{
+	return GridForSlot(nblocks, VariantSlot(s));
+}
+
+/* The launch description of one texture. */
+Job SingleJob(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int blocksW, int nblocks,
+	const nebc7_settings& s, BlockResult* results, int* counter, int* status)
+{
+	Job job;
+	job.tex = nullptr;
+	job.single.dst = dst;
+	job.single.bgra = bgra;
+	job.single.mask = mask;
+	job.single.stride = stride;
+	job.single.blocksW = blocksW;
+	job.single.nblocks = nblocks;
+	job.single.first = 0;
+	job.single.denoise = s.denoise;
+	job.single.P = MakeParams(s);
+	job.ntex = 1;
+	job.total = nblocks;
+	job.results = results;
+	job.counter = counter;
+	job.status = status;
+	return job;
 }
 
 /* Scratch of one encode: the work-queue head and status word, the reduced
@@ -265,17 +295,7 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 	BlockResult* results = wantSums ? (BlockResult*)(scratch + 256) : nullptr;
 	CK(cudaMemsetAsync(scratch, 0, 256, stream));
 
-	Job job;
-	job.dst = dst;
-	job.bgra = bgra;
-	job.mask = mask;
-	job.stride = stride;
-	job.blocksW = blocksW;
-	job.nblocks = nblocks;
-	job.results = results;
-	job.counter = counter;
-	job.status = status;
-	const Params P = MakeParams(s);
+	const Job job = SingleJob(dst, bgra, mask, stride, blocksW, nblocks, s, results, counter, status);
 	const int grid = GridFor(nblocks, s);
 	if (grid <= 0)
 	{
@@ -283,7 +303,7 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 			cudaFreeAsync(scratch, stream);
 		return SetError(NEBC7_ECUDA);
 	}
-	CK(kVariants[VariantSlot(s)].launch(grid, stream, job, *T, P));
+	CK(kVariants[VariantSlot(s)].launch(grid, stream, job, *T, *T));
 
 	int rc = NEBC7_OK;
 	if (wantSums)
@@ -454,6 +474,233 @@ int CoreWeightColor()
 
 } // namespace
 
+/* ---- batches ------------------------------------------------------------ */
+
+namespace {
+
+/* Relative cost of one block by preset (measured block throughput on the
+   1024x1024 and 2048x2048 workloads: draft 1, default 11, precise 400,
+   /slow 480, /data 7200); orders a batch's queue longest first. */
+double BlockCost(const nebc7_settings& s)
+{
+	if (!s.doNormal)
+		return 1.0;
+	if (s.linearData)
+		return 7200.0;
+	if (s.doSlow)
+		return 480.0;
+	if (!s.denoise || s.denoiseStep == 0)
+		return 400.0;
+	return 11.0;
+}
+
+struct BatchGroup
+{
+	int slot;                 /* kernel instantiation */
+	int firstTex, ntex;       /* entries of the schedule's texture table */
+	int queueBase;            /* offset of its queue positions in the results */
+	int total;                /* blocks */
+	int grid;
+};
+
+struct BatchSchedule
+{
+	std::vector<TexDesc> table;      /* host copy, groups contiguous */
+	std::vector<BatchGroup> groups;
+	TexDesc* dTable = nullptr;       /* device copy */
+	cudaGraphExec_t graph = nullptr;
+};
+
+} // namespace
+
+struct nebc7_batch
+{
+	int device = 0;
+	bool fromScratch = false;
+	std::vector<nebc7_texture> tex;
+	int totalBlocks = 0;
+	BatchSchedule sched[2];          /* 0: one mixed launch; 1: one launch per preset group */
+	int chosen = 0;
+	uint8_t* dmem = nullptr;         /* counters, results, sums */
+	int* counters = nullptr;
+	BlockResult* results = nullptr;
+	long long* errs = nullptr;
+	double* ssims = nullptr;
+	cudaStream_t cap = nullptr;      /* capture stream */
+	std::vector<cudaStream_t> side;  /* concurrent preset groups */
+	std::vector<cudaEvent_t> ev;     /* fork / join */
+	const LevelTables* T[2] = { nullptr, nullptr };
+};
+
+namespace {
+
+/* Builds schedule `which` of batch b: the texture table in queue order and
+   its launch groups. */
+void BuildSchedule(nebc7_batch* b, int which)
+{
+	BatchSchedule& S = b->sched[which];
+	const int n = int(b->tex.size());
+	std::vector<int> order(n);
+	for (int i = 0; i < n; i++)
+		order[i] = i;
+	std::vector<double> cost(n);
+	std::vector<int> slot(n);
+	for (int i = 0; i < n; i++)
+	{
+		const nebc7_texture& t = b->tex[i];
+		cost[i] = BlockCost(t.settings) * double(t.w / 4) * double(t.h / 4);
+		slot[i] = which == 0 ? kVariantMixed : VariantSlot(t.settings);
+	}
+	/* group by instantiation (mixed: one group), longest first within it */
+	std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+		if (slot[x] != slot[y])
+			return slot[x] < slot[y];
+		return cost[x] > cost[y];
+	});
+	S.table.clear();
+	S.groups.clear();
+	int queue = 0;
+	for (int j = 0; j < n; j++)
+	{
+		const int i = order[j];
+		const nebc7_texture& t = b->tex[i];
+		if (S.groups.empty() || S.groups.back().slot != slot[i])
+		{
+			BatchGroup g;
+			g.slot = slot[i];
+			g.firstTex = int(S.table.size());
+			g.ntex = 0;
+			g.queueBase = queue;
+			g.total = 0;
+			g.grid = 0;
+			S.groups.push_back(g);
+		}
+		BatchGroup& g = S.groups.back();
+		TexDesc d;
+		d.dst = t.d_dst;
+		d.bgra = t.d_bgra;
+		d.mask = t.d_mask;
+		d.stride = t.stride;
+		d.blocksW = t.w / 4;
+		d.nblocks = (t.w / 4) * (t.h / 4);
+		d.first = g.total;
+		d.denoise = t.settings.denoise;
+		d.id = i;
+		d.P = MakeParams(t.settings);
+		S.table.push_back(d);
+		g.ntex++;
+		g.total += d.nblocks;
+		queue += d.nblocks;
+	}
+	for (BatchGroup& g : S.groups)
+		g.grid = GridForSlot(g.total, g.slot);
+}
+
+/* Enqueues schedule `which` on stream st (capturable): clears the outputs
+   if asked, zeroes the queue heads, launches the groups (concurrently on
+   side streams when there are several) and reduces the per-texture sums. */
+int EnqueueSchedule(nebc7_batch* b, int which, cudaStream_t st)
+{
+	BatchSchedule& S = b->sched[which];
+	if (b->fromScratch)
+		for (const nebc7_texture& t : b->tex)
+			CK(cudaMemsetAsync(t.d_dst, 0, size_t(t.w / 4) * (t.h / 4) * 16, st));
+	CK(cudaMemsetAsync(b->counters, 0, sizeof(int) * 2 * S.groups.size(), st));
+	const int ng = int(S.groups.size());
+	if (ng > 1)
+	{
+		CK(cudaEventRecord(b->ev[0], st));
+		for (int g = 1; g < ng; g++)
+			CK(cudaStreamWaitEvent(b->side[g - 1], b->ev[0], 0));
+	}
+	for (int g = 0; g < ng; g++)
+	{
+		const BatchGroup& G = S.groups[g];
+		if (G.total == 0 || G.grid <= 0)
+			continue;
+		Job job;
+		job.tex = S.dTable + G.firstTex;
+		job.ntex = G.ntex;
+		job.total = G.total;
+		job.results = b->results + G.queueBase;
+		job.counter = b->counters + 2 * g;
+		job.status = b->counters + 2 * g + 1;
+		job.single = S.table[G.firstTex];
+		const cudaStream_t gs = g == 0 ? st : b->side[g - 1];
+		CK(kVariants[G.slot].launch(G.grid, gs, job, *b->T[0], *b->T[1]));
+	}
+	if (ng > 1)
+	{
+		for (int g = 1; g < ng; g++)
+		{
+			CK(cudaEventRecord(b->ev[g], b->side[g - 1]));
+			CK(cudaStreamWaitEvent(st, b->ev[g], 0));
+		}
+	}
+	for (int g = 0; g < ng; g++)
+	{
+		const BatchGroup& G = S.groups[g];
+		if (G.ntex)
+		{
+			/* per-texture sums over the group's queue positions */
+			KReduceTextures<<<G.ntex, 256, 0, st>>>(b->results + G.queueBase, S.dTable + G.firstTex, b->errs, b->ssims);
+			CK(cudaGetLastError());
+		}
+	}
+	return NEBC7_OK;
+}
+
+/* Captures schedule `which` into a CUDA graph (once). */
+int GraphFor(nebc7_batch* b, int which, cudaGraphExec_t* out)
+{
+	BatchSchedule& S = b->sched[which];
+	if (!S.graph)
+	{
+		cudaGraph_t g = nullptr;
+		CK(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal));
+		const int rc = EnqueueSchedule(b, which, b->cap);
+		const cudaError_t e = cudaStreamEndCapture(b->cap, &g);
+		if (rc != NEBC7_OK || e != cudaSuccess)
+		{
+			if (g)
+				cudaGraphDestroy(g);
+			return SetError(rc != NEBC7_OK ? rc : NEBC7_ECUDA);
+		}
+		const cudaError_t ie = cudaGraphInstantiate(&S.graph, g, 0);
+		cudaGraphDestroy(g);
+		if (ie != cudaSuccess)
+		{
+			S.graph = nullptr;
+			return SetError(NEBC7_ECUDA);
+		}
+	}
+	*out = S.graph;
+	return NEBC7_OK;
+}
+
+void FreeBatch(nebc7_batch* b)
+{
+	if (!b)
+		return;
+	cudaSetDevice(b->device);
+	for (BatchSchedule& S : b->sched)
+	{
+		if (S.graph)
+			cudaGraphExecDestroy(S.graph);
+		cudaFree(S.dTable);
+	}
+	for (cudaStream_t s : b->side)
+		cudaStreamDestroy(s);
+	for (cudaEvent_t e : b->ev)
+		cudaEventDestroy(e);
+	if (b->cap)
+		cudaStreamDestroy(b->cap);
+	cudaFree(b->dmem);
+	delete b;
+}
+
+} // namespace
+
 /* ---- allocation-free encode -------------------------------------------- */
 
 /* Largest texture nebc7_encode_device_noalloc accepts: 65536 blocks
@@ -528,18 +775,9 @@ int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uin
 	const cudaStream_t st = (cudaStream_t)stream;
 	/* the queue head and status word must start at zero */
 	CK(cudaMemsetAsync(scratch, 0, 256, st));
-	Job job;
-	job.dst = d_dst;
-	job.bgra = d_bgra;
-	job.mask = d_mask;
-	job.stride = stride;
-	job.blocksW = w / 4;
-	job.nblocks = int(nb);
-	job.results = d_sums ? (BlockResult*)(scratch + 256) : nullptr;
-	job.counter = (int*)scratch;
-	job.status = (int*)scratch + 1;
-	const Params P = MakeParams(*settings);
-	CK(kVariants[VariantSlot(*settings)].launch(grid, st, job, *T, P));
+	const Job job = SingleJob(d_dst, d_bgra, d_mask, stride, w / 4, int(nb), *settings,
+		d_sums ? (BlockResult*)(scratch + 256) : nullptr, (int*)scratch, (int*)scratch + 1);
+	CK(kVariants[VariantSlot(*settings)].launch(grid, st, job, *T, *T));
 	if (d_sums)
 	{
 		KReduceResults<<<1, 256, 0, st>>>(job.results, int(nb), (long long*)d_sums, (double*)((uint8_t*)d_sums + 16));
@@ -749,6 +987,220 @@ int nebc7_init_device(int denoise)
 	CK(cudaGetDevice(&dev));
 	const LevelTables* T = nullptr;
 	return BuildTables(dev, denoise, &T);
+}
+
+int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_batch** out)
+{
+	if (!out || n <= 0 || !textures || (flags & ~NEBC7_BATCH_FROM_SCRATCH))
+		return SetError(NEBC7_EINVAL);
+	*out = nullptr;
+	long long total = 0;
+	for (int i = 0; i < n; i++)
+	{
+		const nebc7_texture& t = textures[i];
+		if (int e = ValidateSettings(&t.settings))
+			return SetError(e);
+		if (t.w <= 0 || t.h <= 0 || (t.w & 3) || (t.h & 3) || t.stride < (long long)t.w * 4 || (t.stride & 3))
+			return SetError(NEBC7_EINVAL);
+		if (!t.d_dst || !t.d_bgra || ((uintptr_t)t.d_dst & 15) || ((uintptr_t)t.d_bgra & 3) || ((uintptr_t)t.d_mask & 3))
+			return SetError(NEBC7_EINVAL);
+		total += (long long)(t.w / 4) * (t.h / 4);
+	}
+	if (total > 0x7FFFFFFF)
+		return SetError(NEBC7_ETOOBIG);
+	nebc7_batch* b = new nebc7_batch;
+	b->fromScratch = (flags & NEBC7_BATCH_FROM_SCRATCH) != 0;
+	b->tex.assign(textures, textures + n);
+	b->totalBlocks = int(total);
+	int rc = NEBC7_OK;
+	if (cudaGetDevice(&b->device) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	for (int d = 0; d < 2 && rc == NEBC7_OK; d++)
+		rc = BuildTables(b->device, d, &b->T[d]);
+	if (rc == NEBC7_OK)
+	{
+		BuildSchedule(b, 0);
+		BuildSchedule(b, 1);
+		const size_t ng = std::max(b->sched[0].groups.size(), b->sched[1].groups.size());
+		const size_t offRes = 256 + ((sizeof(int) * 2 * ng + 255) & ~size_t(255));
+		const size_t offErr = offRes + ((size_t(total) * sizeof(BlockResult) + 255) & ~size_t(255));
+		const size_t bytes = offErr + size_t(n) * 4 * sizeof(long long);
+		if (cudaMalloc((void**)&b->dmem, bytes) != cudaSuccess)
+			rc = SetError(NEBC7_ENOMEM);
+		else
+		{
+			b->counters = (int*)(b->dmem + 256);
+			b->results = (BlockResult*)(b->dmem + offRes);
+			b->errs = (long long*)(b->dmem + offErr);
+			b->ssims = (double*)(b->errs + 2 * n);
+		}
+		for (int w = 0; w < 2 && rc == NEBC7_OK; w++)
+		{
+			BatchSchedule& S = b->sched[w];
+			for (const BatchGroup& g : S.groups)
+				if (g.grid <= 0 && g.total > 0)
+					rc = SetError(NEBC7_ECUDA);
+			if (rc == NEBC7_OK && cudaMalloc((void**)&S.dTable, sizeof(TexDesc) * S.table.size()) != cudaSuccess)
+				rc = SetError(NEBC7_ENOMEM);
+			if (rc == NEBC7_OK && cudaMemcpy(S.dTable, S.table.data(), sizeof(TexDesc) * S.table.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+				rc = SetError(NEBC7_ECUDA);
+		}
+		if (rc == NEBC7_OK && cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking) != cudaSuccess)
+			rc = SetError(NEBC7_ECUDA);
+		for (size_t i = 0; i < ng && rc == NEBC7_OK; i++)
+		{
+			cudaEvent_t e;
+			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+				rc = SetError(NEBC7_ECUDA);
+			else
+				b->ev.push_back(e);
+			if (rc == NEBC7_OK && i > 0)
+			{
+				cudaStream_t s2;
+				if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess)
+					rc = SetError(NEBC7_ECUDA);
+				else
+					b->side.push_back(s2);
+			}
+		}
+	}
+	if (rc != NEBC7_OK)
+	{
+		FreeBatch(b);
+		return rc;
+	}
+	/* without tuning: one launch per preset group when the batch mixes presets */
+	b->chosen = b->sched[1].groups.size() > 1 ? 1 : 0;
+	*out = b;
+	return NEBC7_OK;
+}
+
+int nebc7_batch_tune(nebc7_batch* b, int trials, float* ms_out)
+{
+	if (!b || trials <= 0)
+		return SetError(NEBC7_EINVAL);
+	CK(cudaSetDevice(b->device));
+	/* the trials rewrite the outputs: keep the starting blocks unless every
+	   launch starts from scratch anyway */
+	std::vector<uint8_t*> saved;
+	int rc = NEBC7_OK;
+	if (!b->fromScratch)
+	{
+		for (const nebc7_texture& t : b->tex)
+		{
+			const size_t bytes = size_t(t.w / 4) * (t.h / 4) * 16;
+			uint8_t* p = nullptr;
+			if (cudaMalloc((void**)&p, bytes) != cudaSuccess || cudaMemcpy(p, t.d_dst, bytes, cudaMemcpyDeviceToDevice) != cudaSuccess)
+			{
+				cudaFree(p);
+				rc = SetError(NEBC7_ENOMEM);
+				break;
+			}
+			saved.push_back(p);
+		}
+	}
+	auto restore = [&]() {
+		for (size_t i = 0; i < saved.size(); i++)
+		{
+			const nebc7_texture& t = b->tex[i];
+			cudaMemcpyAsync(t.d_dst, saved[i], size_t(t.w / 4) * (t.h / 4) * 16, cudaMemcpyDeviceToDevice, b->cap);
+		}
+	};
+	float best[2] = { 3.4e38f, 3.4e38f };
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	if (rc == NEBC7_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+		rc = SetError(NEBC7_ECUDA);
+	for (int trial = 0; trial < trials && rc == NEBC7_OK; trial++)
+	{
+		for (int w = 0; w < 2 && rc == NEBC7_OK; w++)
+		{
+			if (w == 1 && b->sched[1].groups.size() < 2)
+				continue;   /* same as the mixed launch */
+			cudaGraphExec_t g = nullptr;
+			rc = GraphFor(b, w, &g);
+			if (rc != NEBC7_OK)
+				break;
+			restore();
+			if (cudaEventRecord(e0, b->cap) != cudaSuccess || cudaGraphLaunch(g, b->cap) != cudaSuccess ||
+				cudaEventRecord(e1, b->cap) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+			{
+				rc = SetError(NEBC7_ECUDA);
+				break;
+			}
+			float ms = 0;
+			cudaEventElapsedTime(&ms, e0, e1);
+			best[w] = std::min(best[w], ms);
+		}
+	}
+	if (rc == NEBC7_OK)
+	{
+		b->chosen = best[1] < best[0] ? 1 : 0;
+		if (ms_out)
+		{
+			ms_out[0] = best[0];
+			ms_out[1] = best[1];
+		}
+	}
+	restore();
+	cudaStreamSynchronize(b->cap);
+	for (uint8_t* p : saved)
+		cudaFree(p);
+	if (e0)
+		cudaEventDestroy(e0);
+	if (e1)
+		cudaEventDestroy(e1);
+	return rc;
+}
+
+int nebc7_batch_launch(nebc7_batch* b, void* stream)
+{
+	if (!b)
+		return SetError(NEBC7_EINVAL);
+	cudaGraphExec_t g = nullptr;
+	if (int rc = GraphFor(b, b->chosen, &g))
+		return rc;
+	CK(cudaGraphLaunch(g, (cudaStream_t)stream));
+	return NEBC7_OK;
+}
+
+int nebc7_batch_sums(nebc7_batch* b, void* stream, int64_t* errs, double* ssim)
+{
+	if (!b)
+		return SetError(NEBC7_EINVAL);
+	const size_t n = b->tex.size();
+	const cudaStream_t st = (cudaStream_t)stream;
+	if (errs)
+		CK(cudaMemcpyAsync(errs, b->errs, sizeof(long long) * 2 * n, cudaMemcpyDeviceToHost, st));
+	if (ssim)
+		CK(cudaMemcpyAsync(ssim, b->ssims, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, st));
+	CK(cudaStreamSynchronize(st));
+	return NEBC7_OK;
+}
+
+int nebc7_batch_set_schedule(nebc7_batch* b, int schedule)
+{
+	if (!b || schedule < 0 || schedule > 1)
+		return SetError(NEBC7_EINVAL);
+	b->chosen = schedule;
+	return NEBC7_OK;
+}
+
+int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* blocks)
+{
+	if (!b)
+		return SetError(NEBC7_EINVAL);
+	if (schedule)
+		*schedule = b->chosen;
+	if (launches)
+		*launches = int(b->sched[b->chosen].groups.size());
+	if (blocks)
+		*blocks = b->totalBlocks;
+	return NEBC7_OK;
+}
+
+void nebc7_batch_destroy(nebc7_batch* b)
+{
+	FreeBatch(b);
 }
 
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)

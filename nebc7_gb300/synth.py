@@ -304,3 +304,26 @@ def random_start_blocks(n: int, seed: int) -> np.ndarray:
     """n arbitrary 16-byte starting blocks (any mode, any bits)."""
     rng = SplitMix64(seed)
     return rng.below(256, n * 16).reshape(n, 16).astype(np.uint8)
+
+
+BATCH_PRESETS = ("draft", "default", "precise")
+
+
+def batch_textures(n: int, seed: int, lo: int = 4, hi: int = 2048) -> list[dict]:
+    """Descriptions of a mixed batch: n textures with sides log-uniform in
+    [lo, hi] (rounded up to x4, non-square), 60 % opaque (photo-like or
+    gradient + noise) and 40 % with alpha (blobs; encoded with the outline
+    mask), presets draft / default / precise in equal shares.  Each entry:
+    {"w", "h", "kind", "seed", "alpha", "preset"}.
+    """
+    sides = texture_sides(n, seed, lo, hi)
+    rng = SplitMix64(seed ^ 0x5EED5EED)
+    kind_draw = rng.below(100, n)
+    preset_draw = rng.below(3, n)
+    out = []
+    for i in range(n):
+        k = int(kind_draw[i])
+        kind = "alpha_blobs" if k < 40 else ("photo_like" if k < 70 else "gradient_noise")
+        out.append({"w": int(sides[i, 0]), "h": int(sides[i, 1]), "kind": kind, "seed": seed * 1000 + i,
+                    "alpha": kind == "alpha_blobs", "preset": BATCH_PRESETS[int(preset_draw[i])]})
+    return out
