@@ -200,12 +200,57 @@ def run_reference_batch(args, world):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_serve(args, world):
+    """CPU arm of the serving mix: the oracle port over requests of the mix
+    (crops of 1024x1024 sources, sides capped at 1024), bounded per step."""
+    from nebc7_gb300 import synth
+    from nebc7_gb300.api import outline_mask
+    from oracle.pyoracle import Port
+    port = Port()
+    sources = {}
+    for name, kind in (("photo", "photo_like"), ("gradient", "gradient_noise"), ("alpha", "alpha_blobs")):
+        img = synth.image_for(kind, 1024, 1024, 11)
+        sources[name] = (img, outline_mask(img, 1) if name == "alpha" else None)
+    reqs = serve_requests(256, 100, {k: (v[0], v[1]) for k, v in sources.items()})
+    threads = os.cpu_count() or 1
+    rates, i = [], 0
+    for step in range(args.warmup + args.steps):
+        spent, done = 0.0, 0
+        while spent < args.cpu_budget / max(1, args.steps):
+            r = reqs[i % len(reqs)]
+            i += 1
+            img, mask = r["src"]
+            w, h = min(r["w"], 1024), min(r["h"], 1024)
+            x0, y0 = min(r["x"], 1024 - w) & ~3, min(r["y"], 1024 - h) & ~3
+            crop = np.ascontiguousarray(img[y0:y0 + h, x0:x0 + w])
+            m = np.ascontiguousarray(mask[y0:y0 + h, x0:x0 + w]) if mask is not None else np.full_like(crop, 255)
+            d, s_, dr, no, sl, li = r["settings"]
+            port.lib.nebc7_oracle_init(d)
+            out = np.zeros(((h // 4) * (w // 4), 16), np.uint8)
+            t0 = time.time()
+            port.compress_texture(out, crop, m, d, s_, dr, no, sl, li, threads=threads)
+            spent += time.time() - t0
+            done += w * h
+        if step >= args.warmup:
+            rates.append(done / spent / 1e6)
+    value = float(np.mean(rates))
+    print(json.dumps({
+        "impl": "reference", "metric": "bc7_encode_Mpx_per_s", "value": value, "unit": "Mpx/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic", "config": {"workload": "serve"},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port",
+                         "sample": "requests of the serving mix (sides capped at 1024), bounded per step"},
+        "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def run_reference(args, rank, world):
     """CPU baseline arm: the oracle port on all host cores, rank 0 only."""
     if rank != 0:
         return
     if args.workload == "batch512":
         return run_reference_batch(args, world)
+    if args.workload == "serve":
+        return run_reference_serve(args, world)
     padded, mask, o, d, s, gkey = prepare(args.workload)
     ph, pw = padded.shape[:2]
     rates = []
@@ -498,13 +543,141 @@ def run_batch(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+SERVE_PRESETS = (("default", (1, 9, 1, 1, 0, 0), 50), ("draft", (1, 9, 1, 0, 0, 0), 30),
+                 ("precise", (0, 0, 1, 1, 0, 0), 15), ("m6i2", (1, 9, 2, 0, 0, 0), 5))
+
+
+def serve_requests(n, seed, sources):
+    """n requests: sides log-uniform 64..4096 per axis (x4), 70 % opaque /
+    30 % alpha crops of the source images, presets default / draft /
+    precise / Mode6Index2 = 50 / 30 / 15 / 5 %."""
+    from nebc7_gb300 import synth
+    sides = synth.texture_sides(n, seed, 64, 4096)
+    rng = synth.SplitMix64(seed ^ 0x5E7E)
+    kind = rng.below(100, n)
+    pres = rng.below(100, n)
+    ox = rng.below(1 << 30, n)
+    oy = rng.below(1 << 30, n)
+    out = []
+    for i in range(n):
+        w, h = int(sides[i, 0]), int(sides[i, 1])
+        src = sources["alpha"] if kind[i] < 30 else (sources["photo"] if kind[i] < 65 else sources["gradient"])
+        img, mask = src
+        x0 = int(ox[i] % (img.shape[1] - w + 1)) & ~3
+        y0 = int(oy[i] % (img.shape[0] - h + 1)) & ~3
+        acc, name, st = 0, None, None
+        for nm, stv, share in SERVE_PRESETS:
+            acc += share
+            if pres[i] < acc:
+                name, st = nm, stv
+                break
+        out.append({"x": x0, "y": y0, "w": w, "h": h, "src": src, "preset": name, "settings": st})
+    return out
+
+
+def run_serve(args, rank, world, local):
+    """Poisson arrivals at 50 / 200 / 800 requests/s into the request loop;
+    latency percentiles and aggregate Mpx/s per rate."""
+    import threading
+    import torch
+    import nebc7_gb300
+    from nebc7_gb300 import Server, synth
+    from nebc7_gb300._native import Settings
+    from nebc7_gb300.api import outline_mask
+
+    torch.cuda.set_device(local)
+    nebc7_gb300.build()
+    lib = nebc7_gb300.load()
+    for d in (0, 1):
+        assert lib.nebc7_init_device(d) == 0
+    # three 4096x4096 sources, pinned; requests are crops (row stride 4096 * 4)
+    sources = {}
+    for name, kind in (("photo", "photo_like"), ("gradient", "gradient_noise"), ("alpha", "alpha_blobs")):
+        img = synth.image_for(kind, 4096, 4096, 11)
+        mask = outline_mask(img, 1) if name == "alpha" else None
+        sources[name] = (torch.from_numpy(img).pin_memory(), torch.from_numpy(mask).pin_memory() if mask is not None else None)
+    results = []
+    n = args.serve_requests
+    for rate_i, rate in enumerate((50.0, 200.0, 800.0)):
+        reqs = serve_requests(n, 100 + rate_i, sources)
+        arrivals = -np.log1p(-np.minimum(synth.SplitMix64(300 + rate_i).u64(n).astype(np.float64) / 2.0 ** 64,
+                                         1 - 1e-12)) / rate
+        arrivals = np.cumsum(arrivals)
+        outs = [torch.empty(((r["h"] // 4) * (r["w"] // 4), 16), dtype=torch.uint8).pin_memory() for r in reqs]
+        srv = Server(hbm_budget=64 << 30, max_batch=64, streams=4)
+        tickets = [None] * n
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, r in enumerate(reqs):
+                delay = t0 + arrivals[i] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                img, mask = r["src"]
+                off = (r["y"] * 4096 + r["x"]) * 4
+                ticket = ctypes.c_int64()
+                st = Settings(*r["settings"])
+                rc = lib.nebc7_server_submit(srv._h, img.data_ptr() + off,
+                                             mask.data_ptr() + off if mask is not None else None, 4096 * 4,
+                                             r["w"], r["h"], ctypes.byref(st), outs[i].data_ptr(), ctypes.byref(ticket))
+                assert rc == 0
+                tickets[i] = ticket.value
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat, done_t = [], []
+        for i in range(n):
+            while tickets[i] is None:
+                time.sleep(0.0005)
+            info = srv.wait(tickets[i])
+            lat.append(info["latency_ms"])
+            done_t.append(time.perf_counter())
+        th.join()
+        wall = max(done_t) - t0
+        stats = srv.stats()
+        srv.close()
+        px = sum(r["w"] * r["h"] for r in reqs)
+        # bit-exact spot check: the first requests against plain host encodes
+        exact = True
+        for i in range(min(6, n)):
+            r = reqs[i]
+            img, mask = r["src"]
+            crop = np.ascontiguousarray(img.numpy()[r["y"]:r["y"] + r["h"], r["x"]:r["x"] + r["w"]])
+            mcrop = np.ascontiguousarray(mask.numpy()[r["y"]:r["y"] + r["h"], r["x"]:r["x"] + r["w"]]) if mask is not None else None
+            ref = np.zeros(((r["h"] // 4) * (r["w"] // 4), 16), np.uint8)
+            st = Settings(*r["settings"])
+            assert lib.nebc7_encode_host(ref.ctypes.data, crop.ctypes.data,
+                                         mcrop.ctypes.data if mcrop is not None else None, r["w"] * 4, r["w"], r["h"],
+                                         ctypes.byref(st), None, None) == 0
+            exact &= bool(np.array_equal(ref, outs[i].numpy()))
+        results.append({"rate_rps": rate, "requests": n, "mpx": px / 1e6, "wall_s": wall,
+                        "value": px / wall / 1e6, "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "p999_ms": float(np.percentile(lat, 99.9)),
+                        "launches": stats["launches"], "peak_bytes": stats["peak_bytes"], "bit_exact_sample": exact})
+    if rank == 0:
+        best = max(results, key=lambda r: r["value"])
+        line = {
+            "metric": "bc7_encode_Mpx_per_s", "value": best["value"], "unit": "Mpx/s", "n_gpus": world,
+            "steps": len(results), "warmup": 0, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8", "data": "synthetic",
+            "config": {"workload": "serve", "arrivals": "Poisson 50 / 200 / 800 req/s", "requests_per_rate": n,
+                       "sides": "log-uniform 64..4096 per axis, x4 (crops of 4096^2 sources)",
+                       "mix": "70% opaque / 30% alpha; default / draft / precise / Mode6Index2 = 50/30/15/5",
+                       "hbm_budget_gb": 64, "max_batch": 64, "streams": 4},
+            "rates": results,
+            "e2e": {"value": best["value"], "unit": "Mpx/s", "note": "host buffers in, blocks back in host memory"},
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + ["batch512", "serve"], default=DEFAULT_WORKLOAD)
+    ap.add_argument("--serve-requests", type=int, default=48, help="requests per arrival rate (serve workload)")
     ap.add_argument("--cpu-budget", type=float, default=12.0, help="seconds of CPU work for the baseline sample")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -512,6 +685,8 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "batch512":
         run_batch(args, rank, world, local)
+    elif args.workload == "serve":
+        run_serve(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

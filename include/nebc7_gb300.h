@@ -104,7 +104,9 @@ typedef struct nebc7_settings
 {
 	int denoise;        /* kDenoise: 0 or 1 */
 	int denoiseStep;    /* kDenoiseStep */
-	int doDraft;        /* bounding-box passes (the CLI always sets this) */
+	int doDraft;        /* bounding-box passes (the CLI always sets this); 2: only the
+	                       Mode6Index2 pass (the "Mode6Index2 fast" run, no refinement;
+	                       no counterpart in the reference) */
 	int doNormal;       /* refinement + full searches of modes 2, 0 / 5, 4, 7 */
 	int doSlow;         /* full searches of every mode */
 	int linearData;     /* /data: equal channel weights */
@@ -217,6 +219,59 @@ int nebc7_batch_set_schedule(nebc7_batch* b, int schedule);
 int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* blocks);
 
 void nebc7_batch_destroy(nebc7_batch* b);
+
+/* ---- serving (no counterpart in the reference) ------------------------- */
+
+typedef struct nebc7_server nebc7_server;
+
+typedef struct nebc7_server_config
+{
+	size_t hbm_budget;   /* device bytes for requests in flight (sources, masks, outputs, per-block results) */
+	int max_batch;       /* requests per launch */
+	int streams;         /* launches in flight at once */
+} nebc7_server_config;
+
+typedef struct nebc7_request_info
+{
+	int status;          /* NEBC7_OK or the error of the request */
+	double queue_ms;     /* submit -> its launch was enqueued */
+	double latency_ms;   /* submit -> its blocks were back in host memory */
+	int64_t errs[2];     /* as nebc7_encode_host reports them */
+	double ssim[2];
+} nebc7_request_info;
+
+typedef struct nebc7_server_counters
+{
+	long long completed, failed, launches, queued, bytes_in_use, peak_bytes;
+} nebc7_server_counters;
+
+/* Starts a request loop on the current device: one device arena of
+   hbm_budget bytes holds the sources, masks, outputs and per-block results
+   of the requests in flight.  A scheduler thread admits requests in
+   arrival order while the arena has room, and starts a batch of admitted
+   requests (one persistent launch over their blocks, presets mixed) on
+   every free stream, so requests that arrive while others run join the
+   device as soon as a stream and memory free up.  Within a launch the
+   cheapest requests are dealt first, and each request returns (its blocks
+   copied back) as soon as its own blocks are done, while the rest of the
+   launch still runs. */
+int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out);
+
+/* Queues one texture (host buffers; pinned memory lets the copies run
+   asynchronously) to be encoded from scratch into host `dst` (w*h/16
+   blocks).  The buffers must stay valid until nebc7_server_wait returns.
+   NEBC7_ETOOBIG if the request alone exceeds the budget. */
+int nebc7_server_submit(nebc7_server* s, const uint8_t* bgra, const uint8_t* mask, long long stride, int w, int h,
+	const nebc7_settings* settings, uint8_t* dst, int64_t* ticket);
+
+/* Waits for a request (timeout_s < 0: without limit; NEBC7_ELIMIT on
+   timeout, the ticket stays valid), fills `info` and releases the ticket. */
+int nebc7_server_wait(nebc7_server* s, int64_t ticket, double timeout_s, nebc7_request_info* info);
+
+int nebc7_server_stats(nebc7_server* s, nebc7_server_counters* out);
+
+/* Finishes the queued and running requests, then frees the server. */
+void nebc7_server_destroy(nebc7_server* s);
 
 /* Persistent-grid sizing of the encode kernel of the default preset
    (kDenoise 1 with the refinement passes): CTAs per SM and warps per CTA. */

@@ -118,6 +118,20 @@ class Texture(ctypes.Structure):
 
 BATCH_FROM_SCRATCH = 1
 
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_size_t), ("max_batch", I), ("streams", I)]
+
+
+class RequestInfo(ctypes.Structure):
+    _fields_ = [("status", I), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("errs", ctypes.c_int64 * 2), ("ssim", ctypes.c_double * 2)]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [("completed", LL), ("failed", LL), ("launches", LL), ("queued", LL), ("bytes_in_use", LL),
+                ("peak_bytes", LL)]
+
 PInitTables = ctypes.CFUNCTYPE(None, ctypes.c_bool, ctypes.c_bool, ctypes.c_bool, ctypes.c_bool)
 PBlockKernel = ctypes.CFUNCTYPE(None, ctypes.POINTER(WorkerItem), ctypes.POINTER(WorkerItem), I,
                                 ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(BlockSSIM))
@@ -155,6 +169,11 @@ SIGNATURES = {
     "nebc7_batch_set_schedule": (I, [VP, I]),
     "nebc7_batch_info": (I, [VP, VP, VP, VP]),
     "nebc7_batch_destroy": (None, [VP]),
+    "nebc7_server_create": (I, [VP, VP]),
+    "nebc7_server_submit": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),
+    "nebc7_server_wait": (I, [VP, ctypes.c_int64, ctypes.c_double, VP]),
+    "nebc7_server_stats": (I, [VP, VP]),
+    "nebc7_server_destroy": (None, [VP]),
 }
 
 

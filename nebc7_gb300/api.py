@@ -312,8 +312,54 @@ class Batch:
             pass
 
 
+class Server:
+    """Request loop on the current device: textures are submitted as they
+    arrive (host buffers) and come back encoded; see nebc7_server_create."""
+
+    def __init__(self, hbm_budget: int = 64 << 30, max_batch: int = 64, streams: int = 4):
+        self._lib = _native.load()
+        cfg = _native.ServerConfig(hbm_budget, max_batch, streams)
+        self._h = ctypes.c_void_p()
+        check(self._lib.nebc7_server_create(ctypes.byref(cfg), ctypes.byref(self._h)), "server_create")
+        self._keep = {}
+
+    def submit(self, bgra: np.ndarray, mask: np.ndarray | None, dst: np.ndarray, settings: Settings) -> int:
+        """Queues one padded texture; `dst` (uint8[w*h/16, 16]) receives the blocks."""
+        h, w = bgra.shape[:2]
+        ticket = ctypes.c_int64()
+        check(self._lib.nebc7_server_submit(self._h, _ptr(bgra), _ptr(mask) if mask is not None else None, w * 4, w, h,
+                                            ctypes.byref(settings), _ptr(dst), ctypes.byref(ticket)), "server_submit")
+        self._keep[ticket.value] = (bgra, mask, dst)
+        return ticket.value
+
+    def wait(self, ticket: int, timeout: float = -1.0) -> dict:
+        info = _native.RequestInfo()
+        rc = self._lib.nebc7_server_wait(self._h, ticket, timeout, ctypes.byref(info))
+        check(rc, "server_wait")
+        self._keep.pop(ticket, None)
+        return {"queue_ms": info.queue_ms, "latency_ms": info.latency_ms, "errs": [info.errs[0], info.errs[1]],
+                "ssim": [info.ssim[0], info.ssim[1]]}
+
+    def stats(self) -> dict:
+        c = _native.ServerCounters()
+        check(self._lib.nebc7_server_stats(self._h, ctypes.byref(c)), "server_stats")
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.nebc7_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 __all__ = [
     "Bc7Core", "Preset", "DEFAULT", "PRECISE", "EncodeStats", "EncodedImage", "NativeError",
     "encode_image", "encode_device", "pad_texture", "outline_mask", "padded_size", "parse_flags",
-    "Batch", "BatchTexture",
+    "Batch", "BatchTexture", "Server",
 ]

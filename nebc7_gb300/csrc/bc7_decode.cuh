@@ -69,7 +69,8 @@ __global__ void KReduceResults(const BlockResult* r, int n, long long* errs, dou
 }
 
 /* Per-texture sums of a batch: CTA t reduces the per-block results of
-   table entry t over its queue positions, with the same fixed tree as
+   table entry t (its own array, or its queue positions of r), with the
+   same fixed tree as
    KReduceResults (so a texture's sums do not depend on the batch), into
    sums[tex[t].id] = { errAlpha, errColor } and ssims[...] = { alpha, color }. */
 __global__ void KReduceTextures(const BlockResult* r, const TexDesc* tex, long long* errs, double* ssims)
@@ -77,7 +78,7 @@ __global__ void KReduceTextures(const BlockResult* r, const TexDesc* tex, long l
 	__shared__ long long sa[256], sc[256];
 	__shared__ double qa[256], qc[256];
 	const TexDesc& d = tex[blockIdx.x];
-	const BlockResult* rr = r + d.first;
+	const BlockResult* rr = d.results ? d.results : r + d.first;
 	const int n = d.nblocks;
 	const int t = threadIdx.x;
 	long long a = 0, c = 0;

@@ -37,6 +37,9 @@ struct TexDesc
 	int first;               /* queue position of its first block */
 	int denoise;             /* kDenoise of its preset */
 	int id;                  /* caller's index of the texture (batches) */
+	BlockResult* results;    /* its per-block results, or null: the launch's array */
+	int* remaining;          /* optional: blocks still to finish (request loop) */
+	int* doneFlag;           /* set to 1 (host-mapped memory) when remaining reaches 0 */
 	Params P;
 };
 
@@ -156,7 +159,14 @@ __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b,
 			}
 			const int water = R.errTotal;
 
-			if (R.errTotal > step)
+			if (P.doDraft == 2)
+			{
+				/* the "Mode6Index2 fast" run: the draft chain reduced to its
+				   first pass (no counterpart in the reference) */
+				if (R.errTotal > step && (kD > 0 || P.denoiseStep > 0))
+					FastMode6<kD, true>(st, R, P, T);
+			}
+			else if (R.errTotal > step)
 			{
 				if (kD > 0 || P.denoiseStep > 0)
 					FastMode6<kD, true>(st, R, P, T);
@@ -176,7 +186,7 @@ __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b,
 				}
 			}
 
-			if (int(int16_t(R.a1.minmax[0])) > 255 - 16)
+			if (P.doDraft != 2 && int(int16_t(R.a1.minmax[0])) > 255 - 16)
 			{
 				const int gate = R.opaqueAlphaError + step;
 				if (R.errTotal > gate)
@@ -195,7 +205,7 @@ __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b,
 				}
 			}
 
-			if (NORMAL && P.doNormal)
+			if (NORMAL && P.doNormal && P.doDraft != 2)
 				NormalPasses<kD>(st, *ss, R, P, T, lane);
 
 			if (water > R.errTotal)
@@ -260,7 +270,7 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 	b.mask = d.mask ? d.mask + base : nullptr;
 	b.stride = d.stride;
 	b.out = d.dst + (long long)local * 16;
-	b.result = job.results ? job.results + k : nullptr;
+	b.result = d.results ? d.results + local : (job.results ? job.results + k : nullptr);
 	const Params P = d.P;
 	if (kD == kAnyDenoise)
 	{
@@ -271,6 +281,18 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 	}
 	else
 		EncodeBlockAt<kD == 1 ? 1 : 0, NORMAL>(st, ss, b, kD ? T1 : T0, P, lane);
+	if (d.remaining && lane == 0)
+	{
+		/* lane 0 wrote the block and its result: publish them, count the block
+		   and let the last one tell the host that the texture is complete */
+		__threadfence();
+		if (atomicSub(d.remaining, 1) == 1)
+		{
+			__threadfence_system();
+			*reinterpret_cast<volatile int*>(d.doneFlag) = 1;
+		}
+	}
+	__syncwarp();
 }
 
 /* Dynamic shared memory of one encode CTA: the per-warp block state and,

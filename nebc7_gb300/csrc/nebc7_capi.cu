@@ -14,8 +14,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
 #include <mutex>
 #include <string.h>
+#include <thread>
+#include <unordered_map>
 #include <vector>
 
 using namespace nebc7;
@@ -149,7 +155,8 @@ Params MakeParams(const nebc7_settings& s)
 
 int ValidateSettings(const nebc7_settings* s)
 {
-	if (!s || (s->denoise != 0 && s->denoise != 1) || s->denoiseStep < 0 || s->denoiseStep > 4096)
+	if (!s || (s->denoise != 0 && s->denoise != 1) || s->denoiseStep < 0 || s->denoiseStep > 4096 || s->doDraft < 0 ||
+		s->doDraft > 2)
 		return NEBC7_EINVAL;
 	if ((s->doNormal || s->doSlow) && !kHasNormalPasses)
 		return NEBC7_EUNSUPPORTED;
@@ -180,7 +187,7 @@ const EncodeVariant kVariants[kNumVariants] = {
    workloads). */
 int VariantSlot(const nebc7_settings& s)
 {
-	if (!s.doNormal)
+	if (!s.doNormal || s.doDraft == 2)
 		return s.denoise ? 2 : 0;
 	if (!s.denoise)
 		return 1;
@@ -248,6 +255,10 @@ Job SingleJob(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long 
 	job.single.nblocks = nblocks;
 	job.single.first = 0;
 	job.single.denoise = s.denoise;
+	job.single.id = 0;
+	job.single.results = nullptr;
+	job.single.remaining = nullptr;
+	job.single.doneFlag = nullptr;
 	job.single.P = MakeParams(s);
 	job.ntex = 1;
 	job.total = nblocks;
@@ -483,7 +494,7 @@ namespace {
    /slow 480, /data 7200); orders a batch's queue longest first. */
 double BlockCost(const nebc7_settings& s)
 {
-	if (!s.doNormal)
+	if (!s.doNormal || s.doDraft == 2)
 		return 1.0;
 	if (s.linearData)
 		return 7200.0;
@@ -586,6 +597,9 @@ void BuildSchedule(nebc7_batch* b, int which)
 		d.first = g.total;
 		d.denoise = t.settings.denoise;
 		d.id = i;
+		d.results = nullptr;
+		d.remaining = nullptr;
+		d.doneFlag = nullptr;
 		d.P = MakeParams(t.settings);
 		S.table.push_back(d);
 		g.ntex++;
@@ -697,6 +711,400 @@ void FreeBatch(nebc7_batch* b)
 		cudaStreamDestroy(b->cap);
 	cudaFree(b->dmem);
 	delete b;
+}
+
+} // namespace
+
+/* ---- serving ------------------------------------------------------------- */
+
+namespace {
+
+double NowSeconds()
+{
+	return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct ServerRequest
+{
+	const uint8_t* bgra;
+	const uint8_t* mask;
+	long long stride;
+	int w, h;
+	nebc7_settings settings;
+	uint8_t* dst;
+	double tSubmit = 0, tLaunch = 0, tDone = 0;
+	int state = 0;               /* 0 queued, 1 admitted, 2 on the device, 3 done, < 0 error code */
+	size_t off = 0, bytes = 0;   /* its part of the arena */
+	int64_t errs[2] = { 0, 0 };
+	double ssim[2] = { 0, 0 };
+};
+
+/* One launch slot: a stream, the batch's texture table and sums. */
+struct ServerSlot
+{
+	cudaStream_t stream = nullptr;   /* the batch's kernel */
+	cudaStream_t copies = nullptr;   /* each request's sums and blocks, as it completes */
+	cudaEvent_t done = nullptr;      /* end of the kernel */
+	bool busy = false;
+	std::vector<int64_t> reqs;
+	std::vector<int> stage;          /* per request: 0 running, 1 copies enqueued, 2 done */
+	std::vector<cudaEvent_t> copied; /* per request: end of its copies */
+	TexDesc* hTable = nullptr;       /* pinned */
+	TexDesc* dTable = nullptr;
+	int* hRemaining = nullptr;       /* pinned staging of the block counts */
+	int* dRemaining = nullptr;
+	int* hFlags = nullptr;           /* host memory the kernel writes (mapped) */
+	int* dFlags = nullptr;
+	long long* hSums = nullptr;      /* pinned: 2 errs + 2 ssim (as bits) per request */
+	long long* dSums = nullptr;
+	int* dCounter = nullptr;
+};
+
+/* First-fit allocator over the arena (offsets, host bookkeeping only). */
+struct ArenaAllocator
+{
+	std::map<size_t, size_t> free;   /* offset -> size */
+	size_t inUse = 0, peak = 0;
+
+	void Init(size_t bytes) { free.clear(); free[0] = bytes; }
+
+	bool Alloc(size_t bytes, size_t* off)
+	{
+		for (auto it = free.begin(); it != free.end(); ++it)
+			if (it->second >= bytes)
+			{
+				*off = it->first;
+				const size_t rest = it->second - bytes;
+				const size_t at = it->first + bytes;
+				free.erase(it);
+				if (rest)
+					free[at] = rest;
+				inUse += bytes;
+				peak = std::max(peak, inUse);
+				return true;
+			}
+		return false;
+	}
+
+	void Free(size_t off, size_t bytes)
+	{
+		inUse -= bytes;
+		auto it = free.emplace(off, bytes).first;
+		auto next = std::next(it);
+		if (next != free.end() && it->first + it->second == next->first)
+		{
+			it->second += next->second;
+			free.erase(next);
+		}
+		if (it != free.begin())
+		{
+			auto prev = std::prev(it);
+			if (prev->first + prev->second == it->first)
+			{
+				prev->second += it->second;
+				free.erase(it);
+			}
+		}
+	}
+};
+
+} // namespace
+
+struct nebc7_server
+{
+	nebc7_server_config cfg{};
+	int device = 0;
+	uint8_t* arena = nullptr;
+	ArenaAllocator alloc;
+	std::mutex mu;
+	std::condition_variable cv;       /* wakes waiters on completion */
+	std::condition_variable work;     /* wakes the scheduler */
+	std::deque<int64_t> queued;
+	std::deque<int64_t> admitted;
+	std::unordered_map<int64_t, ServerRequest> reqs;
+	int64_t nextId = 0;
+	std::vector<ServerSlot> slots;
+	std::thread worker;
+	bool stop = false;
+	const LevelTables* T[2] = { nullptr, nullptr };
+	long long launches = 0, completed = 0, failed = 0;
+};
+
+namespace {
+
+size_t RequestBytes(const ServerRequest& r)
+{
+	const size_t nb = size_t(r.w / 4) * (r.h / 4);
+	const size_t img = size_t(r.w) * 4 * r.h;
+	return Align256(img) + (r.mask ? Align256(img) : 0) + Align256(nb * 16) + Align256(nb * sizeof(BlockResult));
+}
+
+/* Enqueues one batch of admitted requests on a free slot: copies in,
+   clears the outputs, one mixed-preset persistent launch over the batch,
+   per-request sums, copies out; the slot's event marks the end. */
+int LaunchServerBatch(nebc7_server* sv, ServerSlot& slot, std::vector<int64_t>& batch)
+{
+	const cudaStream_t st = slot.stream;
+	/* shortest expected work first: cheap requests finish (and return) while
+	   the expensive ones still run */
+	std::stable_sort(batch.begin(), batch.end(), [&](int64_t x, int64_t y) {
+		const ServerRequest& a = sv->reqs[x];
+		const ServerRequest& b = sv->reqs[y];
+		return BlockCost(a.settings) * double(a.w) * a.h < BlockCost(b.settings) * double(b.w) * b.h;
+	});
+	int total = 0;
+	for (size_t k = 0; k < batch.size(); k++)
+	{
+		ServerRequest& r = sv->reqs[batch[k]];
+		uint8_t* base = sv->arena + r.off;
+		const size_t nb = size_t(r.w / 4) * (r.h / 4);
+		const size_t img = size_t(r.w) * 4 * r.h;
+		uint8_t* dImg = base;
+		uint8_t* dMask = r.mask ? base + Align256(img) : nullptr;
+		uint8_t* dDst = base + Align256(img) + (r.mask ? Align256(img) : 0);
+		BlockResult* dRes = (BlockResult*)(dDst + Align256(nb * 16));
+		CK(cudaMemcpy2DAsync(dImg, size_t(r.w) * 4, r.bgra, size_t(r.stride), size_t(r.w) * 4, size_t(r.h), cudaMemcpyHostToDevice, st));
+		if (r.mask)
+			CK(cudaMemcpy2DAsync(dMask, size_t(r.w) * 4, r.mask, size_t(r.stride), size_t(r.w) * 4, size_t(r.h), cudaMemcpyHostToDevice, st));
+		CK(cudaMemsetAsync(dDst, 0, nb * 16, st));
+		TexDesc& d = slot.hTable[k];
+		d.dst = dDst;
+		d.bgra = dImg;
+		d.mask = dMask;
+		d.stride = (long long)r.w * 4;
+		d.blocksW = r.w / 4;
+		d.nblocks = int(nb);
+		d.first = total;
+		d.denoise = r.settings.denoise;
+		d.id = int(k);
+		d.results = dRes;
+		d.remaining = slot.dRemaining + k;
+		d.doneFlag = slot.dFlags + k;
+		d.P = MakeParams(r.settings);
+		total += int(nb);
+		slot.hRemaining[k] = int(nb);
+		reinterpret_cast<volatile int*>(slot.hFlags)[k] = 0;
+	}
+	CK(cudaMemcpyAsync(slot.dTable, slot.hTable, sizeof(TexDesc) * batch.size(), cudaMemcpyHostToDevice, st));
+	CK(cudaMemcpyAsync(slot.dRemaining, slot.hRemaining, sizeof(int) * batch.size(), cudaMemcpyHostToDevice, st));
+	CK(cudaMemsetAsync(slot.dCounter, 0, 2 * sizeof(int), st));
+	Job job;
+	job.tex = slot.dTable;
+	job.ntex = int(batch.size());
+	job.total = total;
+	job.results = nullptr;
+	job.counter = slot.dCounter;
+	job.status = slot.dCounter + 1;
+	job.single = slot.hTable[0];
+	const int grid = GridForSlot(total, kVariantMixed);
+	if (grid <= 0)
+		return SetError(NEBC7_ECUDA);
+	CK(kVariants[kVariantMixed].launch(grid, st, job, *sv->T[0], *sv->T[1]));
+	CK(cudaEventRecord(slot.done, st));
+	slot.stage.assign(batch.size(), 0);
+	return NEBC7_OK;
+}
+
+/* Request k of a busy slot has all its blocks: reduce its sums and copy its
+   blocks and sums back on the slot's copy stream. */
+int ReturnServerRequest(nebc7_server* sv, ServerSlot& slot, size_t k)
+{
+	const cudaStream_t cs = slot.copies;
+	const int cap = sv->cfg.max_batch;
+	ServerRequest& r = sv->reqs[slot.reqs[k]];
+	const size_t nb = size_t(r.w / 4) * (r.h / 4);
+	KReduceTextures<<<1, 256, 0, cs>>>(nullptr, slot.dTable + k, slot.dSums, (double*)(slot.dSums + 2 * cap));
+	CK(cudaGetLastError());
+	CK(cudaMemcpyAsync(slot.hSums + 2 * k, slot.dSums + 2 * k, 2 * sizeof(long long), cudaMemcpyDeviceToHost, cs));
+	CK(cudaMemcpyAsync(slot.hSums + 2 * cap + 2 * k, slot.dSums + 2 * cap + 2 * k, 2 * sizeof(long long),
+		cudaMemcpyDeviceToHost, cs));
+	CK(cudaMemcpyAsync(r.dst, slot.hTable[k].dst, nb * 16, cudaMemcpyDeviceToHost, cs));
+	CK(cudaEventRecord(slot.copied[k], cs));
+	return NEBC7_OK;
+}
+
+/* Advances the busy slots: returns each request as soon as the kernel has
+   flagged all its blocks, completes it when its copies are done (sums,
+   times, arena space), and frees a slot once its kernel and all its
+   requests are finished.  Called with sv->mu held. */
+void FinishServerRequest(nebc7_server* sv, ServerSlot& slot, size_t k, int rc)
+{
+	const int cap = sv->cfg.max_batch;
+	ServerRequest& r = sv->reqs[slot.reqs[k]];
+	if (rc == NEBC7_OK)
+	{
+		r.errs[0] = slot.hSums[2 * k];
+		r.errs[1] = slot.hSums[2 * k + 1];
+		memcpy(&r.ssim[0], &slot.hSums[2 * cap + 2 * k], sizeof(double));
+		memcpy(&r.ssim[1], &slot.hSums[2 * cap + 2 * k + 1], sizeof(double));
+		r.state = 3;
+		sv->completed++;
+	}
+	else
+	{
+		r.state = -rc;
+		sv->failed++;
+	}
+	r.tDone = NowSeconds();
+	sv->alloc.Free(r.off, r.bytes);
+	slot.stage[k] = 2;
+}
+
+bool ReapServer(nebc7_server* sv)
+{
+	bool any = false;
+	for (ServerSlot& slot : sv->slots)
+	{
+		if (!slot.busy)
+			continue;
+		const cudaError_t kq = cudaEventQuery(slot.done);
+		const bool kernelFailed = kq != cudaSuccess && kq != cudaErrorNotReady;
+		bool all = true;
+		for (size_t k = 0; k < slot.reqs.size(); k++)
+		{
+			if (slot.stage[k] == 0)
+			{
+				if (kernelFailed)
+				{
+					FinishServerRequest(sv, slot, k, NEBC7_ECUDA);
+					any = true;
+					continue;
+				}
+				if (reinterpret_cast<volatile int*>(slot.hFlags)[k] == 1)
+				{
+					const int rc = ReturnServerRequest(sv, slot, k);
+					if (rc != NEBC7_OK)
+						FinishServerRequest(sv, slot, k, rc);
+					else
+						slot.stage[k] = 1;
+					any = true;
+				}
+			}
+			if (slot.stage[k] == 1)
+			{
+				const cudaError_t q = cudaEventQuery(slot.copied[k]);
+				if (q != cudaErrorNotReady)
+				{
+					FinishServerRequest(sv, slot, k, q == cudaSuccess ? NEBC7_OK : NEBC7_ECUDA);
+					any = true;
+				}
+			}
+			all &= slot.stage[k] == 2;
+		}
+		if (all && kq != cudaErrorNotReady)
+		{
+			slot.reqs.clear();
+			slot.busy = false;
+			any = true;
+		}
+	}
+	return any;
+}
+
+/* The scheduler: admits queued requests in arrival order while the arena
+   has room, and starts a batch of admitted requests on every free slot,
+   so that new requests join the device while earlier batches run. */
+void ServerLoop(nebc7_server* sv)
+{
+	cudaSetDevice(sv->device);
+	std::unique_lock<std::mutex> lock(sv->mu);
+	for (;;)
+	{
+		bool progress = ReapServer(sv);
+		if (progress)
+			sv->cv.notify_all();
+		while (!sv->queued.empty())
+		{
+			ServerRequest& r = sv->reqs[sv->queued.front()];
+			if (!sv->alloc.Alloc(r.bytes, &r.off))
+				break;
+			r.state = 1;
+			sv->admitted.push_back(sv->queued.front());
+			sv->queued.pop_front();
+			progress = true;
+		}
+		for (ServerSlot& slot : sv->slots)
+		{
+			if (slot.busy || sv->admitted.empty())
+				continue;
+			std::vector<int64_t> batch;
+			while (!sv->admitted.empty() && int(batch.size()) < sv->cfg.max_batch)
+			{
+				batch.push_back(sv->admitted.front());
+				sv->admitted.pop_front();
+			}
+			const double now = NowSeconds();
+			for (int64_t id : batch)
+			{
+				sv->reqs[id].state = 2;
+				sv->reqs[id].tLaunch = now;
+			}
+			const int rc = LaunchServerBatch(sv, slot, batch);
+			if (rc != NEBC7_OK)
+			{
+				/* nothing of the batch is known to be in flight: wait for the
+				   stream, then fail its requests */
+				cudaStreamSynchronize(slot.stream);
+				for (int64_t id : batch)
+				{
+					ServerRequest& r = sv->reqs[id];
+					r.state = -rc;
+					r.tDone = NowSeconds();
+					sv->alloc.Free(r.off, r.bytes);
+					sv->failed++;
+				}
+				sv->cv.notify_all();
+				continue;
+			}
+			slot.reqs = batch;
+			slot.busy = true;
+			sv->launches++;
+			progress = true;
+		}
+		bool busy = false;
+		for (const ServerSlot& slot : sv->slots)
+			busy |= slot.busy;
+		if (sv->stop && !busy && sv->queued.empty() && sv->admitted.empty())
+			break;
+		if (!progress)
+		{
+			/* poll the device while batches run; sleep until a submit otherwise */
+			if (busy)
+				sv->work.wait_for(lock, std::chrono::microseconds(50));
+			else
+				sv->work.wait(lock, [&] { return sv->stop || !sv->queued.empty(); });
+		}
+	}
+}
+
+void FreeServer(nebc7_server* sv)
+{
+	if (!sv)
+		return;
+	cudaSetDevice(sv->device);
+	for (ServerSlot& slot : sv->slots)
+	{
+		if (slot.stream)
+			cudaStreamSynchronize(slot.stream);
+		if (slot.copies)
+			cudaStreamSynchronize(slot.copies);
+		cudaStreamDestroy(slot.stream);
+		cudaStreamDestroy(slot.copies);
+		cudaEventDestroy(slot.done);
+		for (cudaEvent_t e : slot.copied)
+			if (e)
+				cudaEventDestroy(e);
+		cudaFreeHost(slot.hFlags);
+		cudaFreeHost(slot.hRemaining);
+		cudaFree(slot.dRemaining);
+		cudaFreeHost(slot.hTable);
+		cudaFreeHost(slot.hSums);
+		cudaFree(slot.dTable);
+		cudaFree(slot.dSums);
+		cudaFree(slot.dCounter);
+	}
+	cudaFree(sv->arena);
+	delete sv;
 }
 
 } // namespace
@@ -1201,6 +1609,157 @@ int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* bl
 void nebc7_batch_destroy(nebc7_batch* b)
 {
 	FreeBatch(b);
+}
+
+int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out)
+{
+	if (!cfg || !out || cfg->hbm_budget < 4096 || cfg->max_batch <= 0 || cfg->max_batch > 4096 || cfg->streams <= 0 ||
+		cfg->streams > 64)
+		return SetError(NEBC7_EINVAL);
+	*out = nullptr;
+	nebc7_server* sv = new nebc7_server;
+	sv->cfg = *cfg;
+	int rc = NEBC7_OK;
+	if (cudaGetDevice(&sv->device) != cudaSuccess)
+		rc = SetError(NEBC7_ECUDA);
+	for (int d = 0; d < 2 && rc == NEBC7_OK; d++)
+		rc = BuildTables(sv->device, d, &sv->T[d]);
+	if (rc == NEBC7_OK && cudaMalloc((void**)&sv->arena, cfg->hbm_budget) != cudaSuccess)
+		rc = SetError(NEBC7_ENOMEM);
+	sv->alloc.Init(cfg->hbm_budget);
+	sv->slots.resize(cfg->streams);
+	const int cap = cfg->max_batch;
+	for (ServerSlot& slot : sv->slots)
+	{
+		if (rc != NEBC7_OK)
+			break;
+		slot.copied.assign(cap, nullptr);
+		for (cudaEvent_t& e : slot.copied)
+			if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+				rc = SetError(NEBC7_ECUDA);
+		if (rc == NEBC7_OK && (cudaHostAlloc((void**)&slot.hFlags, sizeof(int) * cap, cudaHostAllocMapped) != cudaSuccess ||
+			cudaHostGetDevicePointer((void**)&slot.dFlags, slot.hFlags, 0) != cudaSuccess ||
+			cudaMallocHost((void**)&slot.hRemaining, sizeof(int) * cap) != cudaSuccess ||
+			cudaMalloc((void**)&slot.dRemaining, sizeof(int) * cap) != cudaSuccess ||
+			cudaStreamCreateWithFlags(&slot.copies, cudaStreamNonBlocking) != cudaSuccess))
+			rc = SetError(NEBC7_ENOMEM);
+		if (rc != NEBC7_OK)
+			break;
+		if (cudaStreamCreateWithFlags(&slot.stream, cudaStreamNonBlocking) != cudaSuccess ||
+			cudaEventCreateWithFlags(&slot.done, cudaEventDisableTiming) != cudaSuccess ||
+			cudaMallocHost((void**)&slot.hTable, sizeof(TexDesc) * cap) != cudaSuccess ||
+			cudaMallocHost((void**)&slot.hSums, sizeof(long long) * 4 * cap) != cudaSuccess ||
+			cudaMalloc((void**)&slot.dTable, sizeof(TexDesc) * cap) != cudaSuccess ||
+			cudaMalloc((void**)&slot.dSums, sizeof(long long) * 4 * cap) != cudaSuccess ||
+			cudaMalloc((void**)&slot.dCounter, 256) != cudaSuccess)
+			rc = SetError(NEBC7_ENOMEM);
+	}
+	/* size the mixed kernel's launch before any request arrives */
+	if (rc == NEBC7_OK && GridForSlot(1, kVariantMixed) <= 0)
+		rc = SetError(NEBC7_ECUDA);
+	if (rc != NEBC7_OK)
+	{
+		FreeServer(sv);
+		return rc;
+	}
+	sv->worker = std::thread(ServerLoop, sv);
+	*out = sv;
+	return NEBC7_OK;
+}
+
+int nebc7_server_submit(nebc7_server* sv, const uint8_t* bgra, const uint8_t* mask, long long stride, int w, int h,
+	const nebc7_settings* settings, uint8_t* dst, int64_t* ticket)
+{
+	if (!sv || !ticket || !bgra || !dst)
+		return SetError(NEBC7_EINVAL);
+	if (int e = ValidateSettings(settings))
+		return SetError(e);
+	if (w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4)
+		return SetError(NEBC7_EINVAL);
+	if ((long long)(w / 4) * (h / 4) > 0x7FFFFFFF)
+		return SetError(NEBC7_ETOOBIG);
+	ServerRequest r;
+	r.bgra = bgra;
+	r.mask = mask;
+	r.stride = stride;
+	r.w = w;
+	r.h = h;
+	r.settings = *settings;
+	r.dst = dst;
+	r.bytes = RequestBytes(r);
+	if (r.bytes > sv->cfg.hbm_budget)
+		return SetError(NEBC7_ETOOBIG);
+	r.tSubmit = NowSeconds();
+	{
+		std::lock_guard<std::mutex> lock(sv->mu);
+		if (sv->stop)
+			return SetError(NEBC7_EINVAL);
+		const int64_t id = sv->nextId++;
+		sv->reqs.emplace(id, r);
+		sv->queued.push_back(id);
+		*ticket = id;
+	}
+	sv->work.notify_one();
+	return NEBC7_OK;
+}
+
+int nebc7_server_wait(nebc7_server* sv, int64_t ticket, double timeout_s, nebc7_request_info* info)
+{
+	if (!sv)
+		return SetError(NEBC7_EINVAL);
+	std::unique_lock<std::mutex> lock(sv->mu);
+	auto it = sv->reqs.find(ticket);
+	if (it == sv->reqs.end())
+		return SetError(NEBC7_EINVAL);
+	/* elements of the map keep their address while others are inserted */
+	const ServerRequest* rp = &it->second;
+	const auto done = [&] { return rp->state == 3 || rp->state < 0; };
+	if (timeout_s < 0)
+		sv->cv.wait(lock, done);
+	else if (!sv->cv.wait_for(lock, std::chrono::duration<double>(timeout_s), done))
+		return NEBC7_ELIMIT;
+	const ServerRequest& r = *rp;
+	const int rc = r.state < 0 ? -r.state : NEBC7_OK;
+	if (info)
+	{
+		info->status = rc;
+		info->queue_ms = (r.tLaunch - r.tSubmit) * 1e3;
+		info->latency_ms = (r.tDone - r.tSubmit) * 1e3;
+		info->errs[0] = r.errs[0];
+		info->errs[1] = r.errs[1];
+		info->ssim[0] = r.ssim[0];
+		info->ssim[1] = r.ssim[1];
+	}
+	sv->reqs.erase(ticket);
+	return rc;
+}
+
+int nebc7_server_stats(nebc7_server* sv, nebc7_server_counters* out)
+{
+	if (!sv || !out)
+		return SetError(NEBC7_EINVAL);
+	std::lock_guard<std::mutex> lock(sv->mu);
+	out->completed = sv->completed;
+	out->failed = sv->failed;
+	out->launches = sv->launches;
+	out->queued = (long long)sv->queued.size();
+	out->bytes_in_use = (long long)sv->alloc.inUse;
+	out->peak_bytes = (long long)sv->alloc.peak;
+	return NEBC7_OK;
+}
+
+void nebc7_server_destroy(nebc7_server* sv)
+{
+	if (!sv)
+		return;
+	{
+		std::lock_guard<std::mutex> lock(sv->mu);
+		sv->stop = true;
+	}
+	sv->work.notify_all();
+	if (sv->worker.joinable())
+		sv->worker.join();
+	FreeServer(sv);
 }
 
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)

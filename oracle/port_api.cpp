@@ -112,6 +112,7 @@ int nebc7_oracle_compress_texture(uint8_t* dst, const uint8_t* bgra, const uint8
 		return 1;
 	Config cfg;
 	MakeConfig(cfg, denoise, denoiseStep, doDraft != 0, doNormal != 0, doSlow != 0, linearData != 0);
+	cfg.mode6Index2Only = doDraft == 2;   /* doDraft 2: the Mode6Index2-only draft chain */
 	const int bw = w / 4;
 	const int nblocks = bw * (h / 4);
 	JobSums total;
@@ -148,6 +149,7 @@ int nebc7_oracle_compress_blocks(const uint8_t* cells, const uint8_t* masks, uin
 		return 1;
 	Config cfg;
 	MakeConfig(cfg, denoise, denoiseStep, doDraft != 0, doNormal != 0, doSlow != 0, linearData != 0);
+	cfg.mode6Index2Only = doDraft == 2;   /* doDraft 2: the Mode6Index2-only draft chain */
 	JobSums total;
 	ParallelJobs(n, threads, [&](Cell& cell, int k, JobSums& s) {
 		LoadCell(cell, cells + size_t(k) * 64, masks + size_t(k) * 64, 16);

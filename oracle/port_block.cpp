@@ -378,7 +378,14 @@ void CompressBlock(const Config& cfg, uint8_t output[16], Cell& input)
 
 			const int water = input.errTotal;
 
-			if (input.errTotal > denoiseStep)
+			if (cfg.mode6Index2Only)
+			{
+				/* the "Mode6Index2 fast" run: the draft chain reduced to its
+				   first pass (no counterpart in the reference) */
+				if (input.errTotal > denoiseStep && (cfg.denoise > 0 || cfg.denoiseStep > 0))
+					mode6i2::Fast(cfg, input);
+			}
+			else if (input.errTotal > denoiseStep)
 			{
 				if (cfg.denoise > 0 || cfg.denoiseStep > 0)
 					mode6i2::Fast(cfg, input);
@@ -398,7 +405,7 @@ void CompressBlock(const Config& cfg, uint8_t output[16], Cell& input)
 				}
 			}
 
-			if (int16_t(input.area1.minmax[0]) > (255 - 16))
+			if (!cfg.mode6Index2Only && int16_t(input.area1.minmax[0]) > (255 - 16))
 			{
 				const int gate = input.opaqueAlphaError + denoiseStep;
 				if (input.errTotal > gate)
@@ -417,7 +424,7 @@ void CompressBlock(const Config& cfg, uint8_t output[16], Cell& input)
 				}
 			}
 
-			if (cfg.doNormal)
+			if (cfg.doNormal && !cfg.mode6Index2Only)
 			{
 				switch (input.bestMode)
 				{

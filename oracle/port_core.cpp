@@ -19,6 +19,7 @@ void MakeConfig(Config& cfg, int denoise, int denoiseStep, bool doDraft, bool do
 	cfg.denoise = denoise;
 	cfg.denoiseStep = denoiseStep;
 	cfg.doDraft = doDraft;
+	cfg.mode6Index2Only = false;
 	cfg.doNormal = doNormal;
 	cfg.doSlow = doSlow;
 	/* src/Bc7Tables.cpp:789-808 */

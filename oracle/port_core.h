@@ -37,6 +37,7 @@ struct Config
 	int denoise;       /* kDenoise: 0 or 1 */
 	int denoiseStep;   /* kDenoiseStep: 0 or 9 */
 	bool doDraft, doNormal, doSlow;
+	bool mode6Index2Only;   /* draft chain reduced to Mode6Index2 (no counterpart in the reference) */
 	int wA, wG, wR, wB, wColor, wColorAlpha;
 	const LevelTables* lt;
 	const Selection* sel;

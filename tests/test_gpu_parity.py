@@ -70,7 +70,7 @@ def test_blocks_match_reference(native, golden, blocks_input, name):
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
 @pytest.mark.parametrize("preset", [(1, 9), (0, 0)])
-@pytest.mark.parametrize("passes", [(1, 0, 0), (1, 1, 0), (1, 1, 1)])
+@pytest.mark.parametrize("passes", [(1, 0, 0), (1, 1, 0), (1, 1, 1), (2, 0, 0)])
 def test_blocks_match_oracle(native, port, seed, preset, passes):
     n = 3000
     cells, masks = synth.random_blocks(n, 1000 + seed)

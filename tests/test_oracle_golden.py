@@ -91,3 +91,17 @@ def test_port_tables_match_reference():
             b = p.lib.nebc7_oracle_table(d, tid, ctypes.byref(n2))
             assert n1.value == n2.value
             assert ctypes.string_at(a, n1.value) == ctypes.string_at(b, n2.value), (d, tid)
+
+
+def test_port_mode6index2_only_run(port, blocks_input):
+    """The "Mode6Index2 fast" run (doDraft 2, no counterpart in the reference):
+    every block stays the starting block or becomes a mode 6 block, and the
+    error is never below the full draft chain's."""
+    cells, masks, _ = blocks_input
+    io6 = np.zeros((len(cells), 16), np.uint8)
+    e6, _ = port.compress_blocks(cells, masks, io6, 1, 9, 2, 0, 0, 0, threads=4)
+    iod = np.zeros_like(io6)
+    ed, _ = port.compress_blocks(cells, masks, iod, 1, 9, 1, 0, 0, 0, threads=4)
+    assert np.all((io6[:, 0] & 0x7F) == 0x40)          # mode 6 (or the zero mode-6 start)
+    assert int(e6.sum()) >= int(ed.sum())
+    assert not np.array_equal(io6, iod)
