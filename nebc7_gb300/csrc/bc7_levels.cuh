@@ -127,6 +127,22 @@ __device__ __forceinline__ unsigned MergeTop(unsigned list, unsigned batch, int 
 	return lane < N ? m : 0xFFFFFFFFu;
 }
 
+/* The distinct values of channel `offset` among the first `count` pixels,
+   with their multiplicities, into uniq[] (value | count << 16); returns how
+   many.  The scans sum a candidate's error once per distinct value (the
+   integer sums, and so the saturated ones, are the same). */
+__device__ __forceinline__ int UniqueValues(const Area& ar, int count, int offset, int* uniq, int lane)
+{
+	const int x = lane < count ? int(ar.px[lane & 15][offset]) : -1 - lane;
+	const unsigned peers = __match_any_sync(kFull, x);
+	const bool leader = lane < count && (__ffs(peers) - 1) == lane;
+	const unsigned lm = __ballot_sync(kFull, leader);
+	if (leader)
+		uniq[__popc(lm & ((1u << lane) - 1))] = x | (__popc(peers) << 16);
+	__syncwarp();
+	return __popc(lm);
+}
+
 /* Sets node 0 (a zero-error candidate) of a list. */
 __device__ __forceinline__ ChanList ZeroList(int2* nodes, int color, int lane)
 {
@@ -139,7 +155,7 @@ __device__ __forceinline__ ChanList ZeroList(int2* nodes, int color, int lane)
 /* LevelsBuffer and LevelsBufferHalf: writes up to maxSize nodes (err, color). */
 template<int kD, bool HALF>
 __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight,
-	int water, int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int lane)
+	int water, int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int* uniq, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
 	const int shift = bits + int(pbits >= 0 || HALF);
@@ -181,6 +197,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	const bool topNeg = HALF && top < 0;   /* signed compare rejects everything */
 
 	const int rowSize = HALF ? (1 << (2 * shift - 1)) : (1 << (2 * shift));
+	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 	const bool pvar = HALF || pbits >= 0;
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
 	const int pL = reverse ? (pbits >> 8) : (pbits & 1);
@@ -226,15 +243,16 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 			if (on)
 			{
 				unsigned s = 0;
-				for (int i = 0; i < count; i++)
+				for (int u = 0; u < nu; u++)
 				{
-					const int x = ar.px[i][offset];
+					const int e = uniq[u];
+					const int x = e & 0xFFFF;
 					unsigned v;
 					if (HALF)
 						v = (table[size_t(x) * rowSize + (cc >> 1)] >> ((cc & 1) << 2)) & 0xF;
 					else
 						v = table[size_t(x) * rowSize + cc];
-					s += v * v;
+					s += unsigned(e >> 16) * v * v;
 				}
 				if (!HALF && s > 0xFFFF)
 					s = 0xFFFF;
@@ -269,16 +287,16 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
    refinement (the common case of the default preset) inlines the scan. */
 template<int kD, bool HALF>
 __device__ NEBC7_SHARED ChanList ChannelLevels(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
-	int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int lane)
+	int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int* uniq, int lane)
 {
-	return ChannelLevelsScan<kD, HALF>(nodes, ar, ai, offset, weight, water, bits, pbits, transparent, table, maxSize, lane);
+	return ChannelLevelsScan<kD, HALF>(nodes, ar, ai, offset, weight, water, bits, pbits, transparent, table, maxSize, uniq, lane);
 }
 
 /* Single best candidate over the narrower window of the alpha slot of modes
    4 and 5 (src/SnippetLevelsBuffer.h:148-188, 433-490). */
 template<int kD>
 __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
-	int bits, bool transparent, const uint8_t* table, int lane)
+	int bits, bool transparent, const uint8_t* table, int* uniq, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
 	const int shift = bits;
@@ -299,6 +317,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 		top = 0xFFFF;
 	const unsigned top16 = unsigned(top) & 0xFFFF;
 	const int rowSize = 1 << (2 * shift);
+	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
 	unsigned best = 0xFFFFFFFFu;
 	/* two rows per batch when only a row's first chunk can be on */
@@ -320,10 +339,11 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 			if (chunkOn && ((mask >> (2 * j)) & 1))
 			{
 				unsigned s = 0;
-				for (int i = 0; i < count; i++)
+				for (int u = 0; u < nu; u++)
 				{
-					const unsigned v = table[size_t(ar.px[i][offset]) * rowSize + cc];
-					s += v * v;
+					const int e = uniq[u];
+					const unsigned v = table[size_t(e & 0xFFFF) * rowSize + cc];
+					s += unsigned(e >> 16) * v * v;
 				}
 				if (s > 0xFFFF)
 					s = 0xFFFF;
@@ -351,7 +371,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
    are visited in order with the running best. */
 template<int kD>
 __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo& ai, int offset, int weight, int water, int bits,
-	bool transparent, const uint8_t* table, const uint16_t* tower, int lane)
+	bool transparent, const uint8_t* table, const uint16_t* tower, int* uniq, int lane)
 {
 	const int shift = bits;
 	const int count = transparent ? ai.active : ai.count;
@@ -374,6 +394,7 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 		top = 0xFFFF;
 	const int rowSize = 1 << (2 * bits);
 	const int towerSize = 1 << bits;
+	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
 	int best = top;
 	for (int base = win.HL; base < win.HH; base += 32)
@@ -384,8 +405,11 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 		if (iHl < win.HH)
 		{
 			unsigned s = 0;
-			for (int i = 0; i < count; i++)
-				s += tower[size_t(ar.px[i][offset]) * towerSize + iHl];
+			for (int u = 0; u < nu; u++)
+			{
+				const int e = uniq[u];
+				s += unsigned(e >> 16) * tower[size_t(e & 0xFFFF) * towerSize + iHl];
+			}
 			rowLb = s > 0xFFFF ? 0xFFFF : s;
 		}
 		const int nrows = min(32, win.HH - base);
@@ -400,10 +424,11 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 			for (int iL = cH, hL = min(win.LH, iH) + cH; iL <= hL; iL += 32)
 			{
 				unsigned s = 0;
-				for (int i = 0; i < count; i++)
+				for (int u = 0; u < nu; u++)
 				{
-					const unsigned v = table[size_t(ar.px[i][offset]) * rowSize + iL + lane];
-					s += v * v;
+					const int e = uniq[u];
+					const unsigned v = table[size_t(e & 0xFFFF) * rowSize + iL + lane];
+					s += unsigned(e >> 16) * v * v;
 				}
 				if (s > 0xFFFF)
 					s = 0xFFFF;

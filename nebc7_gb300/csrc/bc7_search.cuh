@@ -33,6 +33,7 @@ struct __align__(16) SearchState
 	int2 order[64];          /* full searches: (estimate, partition) */
 	int est[64][3][3];       /* per partition, subset, channel (G, R, B) estimates */
 	int lines[64][2];        /* per partition, estimates of subsets 2 and 3 */
+	int uniq[16];            /* distinct channel values of the subset being scanned */
 };
 
 /* ---------------------------------------------------------------------- */
@@ -303,15 +304,15 @@ __device__ bool InitLevels3(SearchState& ss, int v, const Area& ar, const AreaIn
 	int water, const int est[3], ChanList cl[3], int lane)
 {
 	const int pb = Pbits(MODE, v);
-	cl[0] = ChannelLevels<kD, false>(ss.lists[v][0], ar, ai, 1, P.wG, water - est[1] - est[2], sp.bits, pb, false, sp.table, 32, lane);
+	cl[0] = ChannelLevels<kD, false>(ss.lists[v][0], ar, ai, 1, P.wG, water - est[1] - est[2], sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
 	const int min1 = cl[0].minErr;
 	if (min1 >= water)
 		return false;
-	cl[1] = ChannelLevels<kD, false>(ss.lists[v][1], ar, ai, 2, P.wR, water - min1 - est[2], sp.bits, pb, false, sp.table, 32, lane);
+	cl[1] = ChannelLevels<kD, false>(ss.lists[v][1], ar, ai, 2, P.wR, water - min1 - est[2], sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
 	const int min2 = cl[1].minErr;
 	if (min1 + min2 >= water)
 		return false;
-	cl[2] = ChannelLevels<kD, false>(ss.lists[v][2], ar, ai, 3, P.wB, water - min1 - min2, sp.bits, pb, false, sp.table, 32, lane);
+	cl[2] = ChannelLevels<kD, false>(ss.lists[v][2], ar, ai, 3, P.wB, water - min1 - min2, sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
 	return min1 + min2 + cl[2].minErr < water;
 }
 
@@ -394,22 +395,23 @@ __device__ void RefineOpaque(WarpState& st, SearchState& ss, CellRegs& R, const 
 
 /* EstimateLevels of modes 0-3 (src/Bc7CoreMode0.cpp:500-530). */
 template<int kD>
-__device__ int EstimateLevels3(const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp, int water, int est[4], int lane)
+__device__ int EstimateLevels3(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp, int water,
+	int est[4], int lane)
 {
 	int error = 0;
 	if (error < water)
 	{
-		const int l1 = EstimateChannelLevels<kD>(ar, ai, 1, P.wG, water - error, sp.estBits, false, sp.estTable, sp.estTower, lane);
+		const int l1 = EstimateChannelLevels<kD>(ar, ai, 1, P.wG, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
 		est[1] = l1;
 		error += l1;
 		if (error < water)
 		{
-			const int l2 = EstimateChannelLevels<kD>(ar, ai, 2, P.wR, water - error, sp.estBits, false, sp.estTable, sp.estTower, lane);
+			const int l2 = EstimateChannelLevels<kD>(ar, ai, 2, P.wR, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
 			est[2] = l2;
 			error += l2;
 			if (error < water)
 			{
-				const int l3 = EstimateChannelLevels<kD>(ar, ai, 3, P.wB, water - error, sp.estBits, false, sp.estTable, sp.estTower, lane);
+				const int l3 = EstimateChannelLevels<kD>(ar, ai, 3, P.wB, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
 				est[3] = l3;
 				error += l3;
 				if (error < water)
@@ -465,17 +467,17 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
 		int e[3][4];
 		const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 0, lane);
 		const int water1 = R.errTotal - step - R.opaqueAlphaError;
-		const int line1 = EstimateLevels3<kD>(st.sub[0], a1, P, sp, water1, e[0], lane);
+		const int line1 = EstimateLevels3<kD>(ss, st.sub[0], a1, P, sp, water1, e[0], lane);
 		if (line1 < water1)
 		{
 			const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 1, lane);
 			const int water2 = water1 - line1;
-			const int line2 = EstimateLevels3<kD>(st.sub[0], a2, P, sp, water2, e[1], lane);
+			const int line2 = EstimateLevels3<kD>(ss, st.sub[0], a2, P, sp, water2, e[1], lane);
 			if (line2 < water2)
 			{
 				const AreaInfo a3 = BuildSubset<kD>(st, R, P, st.sub[0], 3, p, 2, lane);
 				const int water3 = water2 - line2;
-				const int line3 = EstimateLevels3<kD>(st.sub[0], a3, P, sp, water3, e[2], lane);
+				const int line3 = EstimateLevels3<kD>(ss, st.sub[0], a3, P, sp, water3, e[2], lane);
 				if (line3 < water3)
 				{
 					if (lane == 0)
@@ -571,11 +573,11 @@ __device__ void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, cons
 		const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
 		int line1 = 0, line2 = 0;
 		int w1 = R.errTotal - step - R.opaqueAlphaError - line2;
-		line1 = max(line1, EstimateLevels3<kD>(st.sub[0], a1, P, sp, w1, e1, lane));
+		line1 = max(line1, EstimateLevels3<kD>(ss, st.sub[0], a1, P, sp, w1, e1, lane));
 		if (line1 < w1)
 		{
 			int w2 = w1 - line1;
-			line2 = max(line2, EstimateLevels3<kD>(st.sub[1], a2, P, sp, w2, e2, lane));
+			line2 = max(line2, EstimateLevels3<kD>(ss, st.sub[1], a2, P, sp, w2, e2, lane));
 			if (line2 < w2)
 			{
 				w1 = R.errTotal - step - R.opaqueAlphaError - line2;
@@ -730,15 +732,15 @@ __device__ bool InitLevels4(SearchState& ss, int v, int pbits, const Area& ar, c
 		}
 		else if (MODE == 6)
 		{
-			cl[c] = ChannelLevels<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d4h, 20, lane);
+			cl[c] = ChannelLevels<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d4h, 20, ss.uniq, lane);
 		}
 		else if (MODE == 9)
 		{
-			cl[c] = ChannelLevelsScan<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, 20, lane);
+			cl[c] = ChannelLevelsScan<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, 20, ss.uniq, lane);
 		}
 		else
 		{
-			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, T.d2v6, 20, lane);
+			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, T.d2v6, 20, ss.uniq, lane);
 		}
 		used += cl[c].minErr;
 		if (used >= water)
@@ -864,7 +866,8 @@ __device__ void RefineMode7(WarpState& st, SearchState& ss, CellRegs& R, const P
 
 /* EstimateLevels of mode 7 (src/Bc7CoreMode7.cpp:574-627). */
 template<int kD>
-__device__ int EstimateLevels7(const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, int water, int est[4], int lane)
+__device__ int EstimateLevels7(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, int water,
+	int est[4], int lane)
 {
 	int error = 0;
 	if (error < water)
@@ -876,7 +879,7 @@ __device__ int EstimateLevels7(const Area& ar, const AreaInfo& ai, const Params&
 		}
 		if (!ai.opaque)
 		{
-			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, T.d2v6, T.c2v6, lane);
+			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, T.d2v6, T.c2v6, ss.uniq, lane);
 			est[0] = l0;
 			error += l0;
 		}
@@ -887,7 +890,7 @@ __device__ int EstimateLevels7(const Area& ar, const AreaInfo& ai, const Params&
 		{
 			if (!(error < water))
 				return water;
-			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, T.d2v6, T.c2v6, lane);
+			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, T.d2v6, T.c2v6, ss.uniq, lane);
 			est[c] = l;
 			error += l;
 		}
@@ -916,11 +919,11 @@ __device__ void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Par
 		const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
 		int line1 = 0, line2 = 0;
 		int w1 = R.errTotal - step - line2;
-		line1 = max(line1, EstimateLevels7<kD>(st.sub[0], a1, P, T, w1, e1, lane));
+		line1 = max(line1, EstimateLevels7<kD>(ss, st.sub[0], a1, P, T, w1, e1, lane));
 		if (line1 < w1)
 		{
 			int w2 = w1 - line1;
-			line2 = max(line2, EstimateLevels7<kD>(st.sub[1], a2, P, T, w2, e2, lane));
+			line2 = max(line2, EstimateLevels7<kD>(ss, st.sub[1], a2, P, T, w2, e2, lane));
 			if (line2 < w2)
 			{
 				w1 = R.errTotal - step - line2;
@@ -1082,9 +1085,9 @@ __device__ int CompressRotSubset(WarpState& st, SearchState& ss, const CellRegs&
 		if (c == 0 && ai.opaque)
 			cl[0] = ZeroList(ss.lists[0][0], 0xFFFF, lane);
 		else if (c == a)
-			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, lane);
+			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, ss.uniq, lane);
 		else
-			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, 32, lane);
+			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, 32, ss.uniq, lane);
 		used += cl[c].minErr;
 		if (used >= water)
 			return water;
