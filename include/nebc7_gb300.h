@@ -273,6 +273,35 @@ int nebc7_server_stats(nebc7_server* s, nebc7_server_counters* out);
 /* Finishes the queued and running requests, then frees the server. */
 void nebc7_server_destroy(nebc7_server* s);
 
+/* ---- the driver's steps around the encode, on the device ---------------- */
+
+/* Pads a w x h BGRA image (rows src_stride bytes apart) to the texture size
+   the reference encodes (each side max(4, n) rounded up to 4) by repeating
+   the last column and row (src/Bc7Compress.cpp:397-426), into d_padded
+   (rows 4 * padded width bytes apart).  If d_mask is non-null it receives
+   the mask of the padded texture (same layout, bytes A, G, R, B): the alpha
+   outline of the given radius (src/Bc7Compress.cpp:33-105), or all 0xFF for
+   radius < 0 (/nomask). */
+int nebc7_prepare_device(const uint8_t* d_src, long long src_stride, int w, int h, uint8_t* d_padded, uint8_t* d_mask,
+	int radius, void* stream);
+
+/* The /bad glitch map (src/Worker.cpp:309-451): for each block whose decoded
+   pixels differ from the source by at least 16 / 12 / 16 / 20 (A, G, R, B;
+   16 each with linear weights) in a masked channel, d_out gets the source
+   pixels; other blocks are cleared.  Padded textures, one stride. */
+int nebc7_bad_blocks_device(const uint8_t* d_src, const uint8_t* d_decoded, const uint8_t* d_mask, long long stride, int w, int h,
+	int linear, uint8_t* d_out, void* stream);
+
+/* The /map partition visualisation (src/Bc7Compress.cpp:131-265): rewrites
+   blocks so that decoding them (nebc7_decode_device) shows each block's
+   mode and partition as flat colours. */
+int nebc7_partition_map_device(const uint8_t* d_blocks, uint8_t* d_out, int nblocks, void* stream);
+
+/* The 96-byte KTX 1.1 header the reference writes before the blocks of a
+   w x h image (src/Bc7Compress.cpp:439-463); flip selects the orientation
+   key "T=u" (bottom-up rows) instead of "T=d". */
+int nebc7_ktx_header(int w, int h, int flip, uint8_t* out);
+
 /* Persistent-grid sizing of the encode kernel of the default preset
    (kDenoise 1 with the refinement passes): CTAs per SM and warps per CTA. */
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count);

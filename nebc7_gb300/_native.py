@@ -174,6 +174,10 @@ SIGNATURES = {
     "nebc7_server_wait": (I, [VP, ctypes.c_int64, ctypes.c_double, VP]),
     "nebc7_server_stats": (I, [VP, VP]),
     "nebc7_server_destroy": (None, [VP]),
+    "nebc7_prepare_device": (I, [VP, LL, I, I, VP, VP, I, VP]),
+    "nebc7_bad_blocks_device": (I, [VP, VP, VP, LL, I, I, I, VP, VP]),
+    "nebc7_partition_map_device": (I, [VP, VP, I, VP]),
+    "nebc7_ktx_header": (I, [I, I, I, VP]),
 }
 
 

@@ -312,6 +312,41 @@ class Batch:
             pass
 
 
+KTX_HEADER_BYTES = 96
+
+
+def ktx_header(width: int, height: int, flip: bool = False) -> bytes:
+    """The KTX 1.1 header the reference's driver writes for a BC7 image."""
+    out = (ctypes.c_uint8 * KTX_HEADER_BYTES)()
+    check(_native.load().nebc7_ktx_header(width, height, int(flip), ctypes.cast(out, ctypes.c_void_p)), "ktx_header")
+    return bytes(out)
+
+
+def write_ktx(path: str, blocks: np.ndarray, width: int, height: int, flip: bool = False) -> None:
+    """Saves blocks (uint8[n, 16] of the padded texture) as a .ktx file."""
+    pw, ph = padded_size(width, height)
+    blocks = np.ascontiguousarray(blocks, dtype=np.uint8)
+    if blocks.size != pw * ph:
+        raise ValueError(f"{blocks.size} bytes of blocks for a {pw}x{ph} texture")
+    with open(path, "wb") as f:
+        f.write(ktx_header(width, height, flip))
+        f.write(blocks.tobytes())
+
+
+def read_ktx(path: str) -> tuple[np.ndarray, int, int, bool]:
+    """Loads a .ktx written by write_ktx (or the reference): (blocks, width,
+    height, flip).  The blocks can seed an incremental re-encode (`start`)."""
+    data = open(path, "rb").read()
+    head = np.frombuffer(data[:KTX_HEADER_BYTES], np.uint32)
+    if len(data) < KTX_HEADER_BYTES or head[0] != 0x58544BAB or head[7] != 0x8E8C:
+        raise ValueError(f"{path}: not a BC7 KTX file")
+    width, height = int(head[9]), int(head[10])
+    size = int(head[23])
+    flip = int(head[22]) == 0x00753D
+    blocks = np.frombuffer(data[KTX_HEADER_BYTES:KTX_HEADER_BYTES + size], np.uint8).reshape(-1, 16).copy()
+    return blocks, width, height, flip
+
+
 class Server:
     """Request loop on the current device: textures are submitted as they
     arrive (host buffers) and come back encoded; see nebc7_server_create."""
@@ -361,5 +396,5 @@ class Server:
 __all__ = [
     "Bc7Core", "Preset", "DEFAULT", "PRECISE", "EncodeStats", "EncodedImage", "NativeError",
     "encode_image", "encode_device", "pad_texture", "outline_mask", "padded_size", "parse_flags",
-    "Batch", "BatchTexture", "Server",
+    "Batch", "BatchTexture", "Server", "ktx_header", "write_ktx", "read_ktx",
 ]

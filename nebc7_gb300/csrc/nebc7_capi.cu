@@ -8,6 +8,7 @@
  */
 #include "bc7_tables.cuh"
 #include "bc7_decode.cuh"
+#include "bc7_tools.cuh"
 
 #include "../../include/nebc7_gb300.h"
 
@@ -1760,6 +1761,73 @@ void nebc7_server_destroy(nebc7_server* sv)
 	if (sv->worker.joinable())
 		sv->worker.join();
 	FreeServer(sv);
+}
+
+int nebc7_prepare_device(const uint8_t* d_src, long long src_stride, int w, int h, uint8_t* d_padded, uint8_t* d_mask,
+	int radius, void* stream)
+{
+	if (!d_src || !d_padded || w <= 0 || h <= 0 || src_stride < (long long)w * 4 || (src_stride & 3) ||
+		((uintptr_t)d_src & 3) || ((uintptr_t)d_padded & 3) || ((uintptr_t)d_mask & 3))
+		return SetError(NEBC7_EINVAL);
+	const int pw = (std::max(4, w) + 3) & ~3, ph = (std::max(4, h) + 3) & ~3;
+	if (std::max(pw, ph) > 16384)
+		return SetError(NEBC7_ETOOBIG);
+	const cudaStream_t st = (cudaStream_t)stream;
+	const dim3 grid((pw + 255) / 256, ph);
+	KPadTexture<<<grid, 256, 0, st>>>(d_src, src_stride, w, h, d_padded, (long long)pw * 4, pw, ph);
+	CK(cudaGetLastError());
+	if (d_mask)
+	{
+		KOutlineMask<<<grid, 256, 0, st>>>(d_padded, (long long)pw * 4, pw, ph, radius, d_mask);
+		CK(cudaGetLastError());
+	}
+	return NEBC7_OK;
+}
+
+int nebc7_bad_blocks_device(const uint8_t* d_src, const uint8_t* d_decoded, const uint8_t* d_mask, long long stride, int w, int h,
+	int linear, uint8_t* d_out, void* stream)
+{
+	if (!d_src || !d_decoded || !d_out || w <= 0 || h <= 0 || (w & 3) || (h & 3) || stride < (long long)w * 4 || (stride & 3) ||
+		((uintptr_t)d_src & 3) || ((uintptr_t)d_decoded & 3) || ((uintptr_t)d_mask & 3) || ((uintptr_t)d_out & 3))
+		return SetError(NEBC7_EINVAL);
+	const dim3 grid((w / 4 + 1) / 2, h / 4);
+	KBadBlocks<<<grid, 32, 0, (cudaStream_t)stream>>>(d_src, d_decoded, d_mask, stride, w, h, linear, d_out);
+	CK(cudaGetLastError());
+	return NEBC7_OK;
+}
+
+int nebc7_partition_map_device(const uint8_t* d_blocks, uint8_t* d_out, int nblocks, void* stream)
+{
+	if (!d_blocks || !d_out || nblocks < 0 || ((uintptr_t)d_blocks & 15) || ((uintptr_t)d_out & 15))
+		return SetError(NEBC7_EINVAL);
+	if (nblocks == 0)
+		return NEBC7_OK;
+	KPartitionMap<<<(nblocks + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_blocks, d_out, nblocks);
+	CK(cudaGetLastError());
+	return NEBC7_OK;
+}
+
+int nebc7_ktx_header(int w, int h, int flip, uint8_t* out)
+{
+	if (!out || w <= 0 || h <= 0 || std::max(w, h) > 16384)
+		return SetError(NEBC7_EINVAL);
+	const int pw = (std::max(4, w) + 3) & ~3, ph = (std::max(4, h) + 3) & ~3;
+	/* KTX 1.1: identifier, endianness, GL format fields (BPTC RGBA, base
+	   RGBA), image size in pixels, one face / level, an orientation
+	   key/value ("KTXOrientation": "S=r,T=u" flipped, "S=r,T=d" otherwise),
+	   then the level's
+	   byte count: the layout the reference writes (src/Bc7Compress.cpp:439-463) */
+	const uint32_t head[24] = {
+		0x58544BABu, 0xBB313120u, 0x0A1A0A0Du, 0x04030201u,
+		0, 1, 0, 0x8E8C, 0x1908,
+		uint32_t(w), uint32_t(h), 0, 0, 1, 1,
+		0x1C, 0x17, 0x4F58544Bu, 0x6E656972u, 0x69746174u, 0x53006E6Fu, 0x542C723Du, flip ? 0x00753Du : 0x00643Du,
+		uint32_t(pw) * uint32_t(ph),
+	};
+	for (int i = 0; i < 24; i++)
+		for (int b = 0; b < 4; b++)
+			out[4 * i + b] = uint8_t(head[i] >> (8 * b));
+	return NEBC7_OK;
 }
 
 int nebc7_launch_shape(int* ctas_per_sm, int* warps_per_cta, int* sm_count)
