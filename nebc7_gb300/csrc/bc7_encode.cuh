@@ -261,7 +261,13 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 				hi = mid - 1;
 		}
 	}
-	const TexDesc& d = job.tex ? job.tex[t] : job.single;
+	/* a copy, read from the table or from the launch's parameters (no
+	   pointer into the parameters, which would put them in local memory) */
+	TexDesc d;
+	if (job.tex)
+		d = job.tex[t];
+	else
+		d = job.single;
 	const int local = k - d.first;
 	const int bx = local % d.blocksW, by = local / d.blocksW;
 	const long long base = (long long)by * 4 * d.stride + (long long)bx * 16;
@@ -313,12 +319,19 @@ constexpr size_t EncodeSharedBytes()
 constexpr int kShapeCompact = 0;
 constexpr int kShapeOutlined = 1;
 
+/* Resident CTAs per SM the compact refining kernel is compiled for (bounds
+   its registers per thread; the draft-only kernels and the outlined shape
+   are compiled for 4). */
+#ifndef NEBC7_COMPACT_MIN_CTAS
+#define NEBC7_COMPACT_MIN_CTAS 1
+#endif
+
 /* Persistent encode kernel over a launch's textures.  NORMAL compiles the
    refinement / full-search passes (run for textures whose preset asks for
    them); only that instantiation reserves the per-warp search state in
    shared memory.  kD: the kDenoise of every texture, or kAnyDenoise. */
 template<int kD, bool NORMAL, int SHAPE>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, SHAPE == kShapeOutlined ? 4 : 1)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, (SHAPE == kShapeOutlined || !NORMAL) ? 4 : NEBC7_COMPACT_MIN_CTAS)
 	KEncode(Job job, LevelTables T0, LevelTables T1)
 {
 	extern __shared__ __align__(16) unsigned char encodeSmem[];
