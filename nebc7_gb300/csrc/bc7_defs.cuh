@@ -19,6 +19,13 @@ namespace nebc7 {
 #define NEBC7_SHARED __noinline__
 #endif
 
+/* Marks the passes a block runs once (the fast passes, the final pack).  The
+   draft-only translation units define it __noinline__; in the kernels with
+   the searches, out-of-line copies raise the register count (232 -> 247). */
+#ifndef NEBC7_ONCE
+#define NEBC7_ONCE
+#endif
+
 
 static __constant__ int c_interp2[4] = { 0, 21, 43, 64 };
 static __constant__ int c_interp3[8] = { 0, 9, 18, 27, 37, 46, 55, 64 };

@@ -187,7 +187,7 @@ __device__ __forceinline__ int AcceptScan(const WarpState& st, int n, int& T, in
 
 /* Modes 0-3: opaque subsets, errors over G, R, B. */
 template<int kD, int MODE>
-__device__ void FastOpaque(WarpState& st, CellRegs& R, const Params& P, int lane)
+__device__ NEBC7_ONCE void FastOpaque(WarpState& st, CellRegs& R, const Params& P, int lane)
 {
 	constexpr int NS = (MODE == 0 || MODE == 2) ? 3 : 2;
 	constexpr int NP = MODE == 0 ? 16 : 64;
@@ -267,7 +267,7 @@ __device__ void FastOpaque(WarpState& st, CellRegs& R, const Params& P, int lane
 
 /* Mode 7: two RGBA subsets with the transparent-alpha term. */
 template<int kD>
-__device__ void FastMode7(WarpState& st, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_ONCE void FastMode7(WarpState& st, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	const int step = R.denoiseStep;
 	const int w[4] = { P.wA, P.wG, P.wR, P.wB };
@@ -307,7 +307,7 @@ __device__ void FastMode7(WarpState& st, CellRegs& R, const Params& P, const Lev
 
 /* Modes 4 and 5: one subset (Area1) per rotation. */
 template<int kD, int MODE>
-__device__ void FastRot(WarpState& st, CellRegs& R, const Params& P, int lane)
+__device__ NEBC7_ONCE void FastRot(WarpState& st, CellRegs& R, const Params& P, int lane)
 {
 	constexpr int NR = MODE == 4 ? 8 : 4;
 	const int step = R.denoiseStep;
@@ -349,7 +349,7 @@ __device__ void FastRot(WarpState& st, CellRegs& R, const Params& P, int lane)
 
 /* Modes 6 and 6Index2: one candidate. */
 template<int kD, bool INDEX2>
-__device__ void FastMode6(WarpState& st, CellRegs& R, const Params& P, const LevelTables& T)
+__device__ NEBC7_ONCE void FastMode6(WarpState& st, CellRegs& R, const Params& P, const LevelTables& T)
 {
 	const int step = R.denoiseStep;
 	const int w[4] = { P.wA, P.wG, P.wR, P.wB };
@@ -700,7 +700,7 @@ __device__ void FinalPackMode6(WarpState& st, CellRegs& R, const Params& P, uint
 }
 
 template<int kD>
-__device__ void FinalPack(WarpState& st, CellRegs& R, const Params& P, uint64_t& lo, uint64_t& hi, int lane)
+__device__ NEBC7_ONCE void FinalPack(WarpState& st, CellRegs& R, const Params& P, uint64_t& lo, uint64_t& hi, int lane)
 {
 	switch (R.bestMode)
 	{
