@@ -791,7 +791,7 @@ __device__ __forceinline__ int TransparentError4(const LevelTables& T, const Par
 	if (e)
 	{
 		e *= P.wA;
-		const int v = (T.d4h[(alpha & 0xFFFF) >> 1] >> ((alpha & 1) << 2)) & 0xF;
+		const int v = HalfAt(T.d4h, 0, alpha & 0xFF, (alpha >> 8) & 0xFF);
 		e *= v * v;
 	}
 	return e;

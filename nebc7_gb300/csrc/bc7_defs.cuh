@@ -84,8 +84,8 @@ struct LevelTables
 	const uint8_t* d3v5;   /* [256][32*32]   */
 	const uint16_t* c3v7s; /* [256][128]     */
 	const uint16_t* c3v5;  /* [256][32]      */
-	const uint8_t* d4h;    /* [256][256*128] nibbles */
-	const uint8_t* d2h;    /* [256][256*128] nibbles */
+	const uint8_t* d4h;    /* [511][256] nibbles, by differences (HalfAt) */
+	const uint8_t* d2h;    /* [511][256] nibbles, by differences (HalfAt) */
 };
 
 /* Per-launch encoder settings: the reference's InitTables flags
@@ -116,6 +116,18 @@ __device__ __forceinline__ int MaxColorError()
 __device__ __forceinline__ int Interp(int e0, int e1, int w)
 {
 	return (e0 * (64 - w) + e1 * w + 32) >> 6;
+}
+
+/* Entry (x, cL, cH) of a nibble table: the quantised distance from x to the
+   nearest level of the 8-bit endpoint pair, clamped to 15.  The levels are
+   cL + (((cH - cL) w + 32) >> 6), so the entry depends on cH - x and cL - x
+   only: one 511 x 511 table serves every x (row cH - x + 255, nibble
+   cL - x + 255), 128 KB instead of 256 rows of 32 KB, and the rows a block
+   touches stay in L1. */
+__device__ __forceinline__ int HalfAt(const uint8_t* table, int x, int cL, int cH)
+{
+	const int a = cH - x + 255, b = cL - x + 255;
+	return (table[a * 256 + (b >> 1)] >> ((b & 1) << 2)) & 0xF;
 }
 
 __device__ __forceinline__ const int* InterpWeights(int bits)

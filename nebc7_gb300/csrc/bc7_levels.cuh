@@ -137,10 +137,15 @@ __device__ __forceinline__ int UniqueValues(const Area& ar, int count, int offse
 	const unsigned peers = __match_any_sync(kFull, x);
 	const bool leader = lane < count && (__ffs(peers) - 1) == lane;
 	const unsigned lm = __ballot_sync(kFull, leader);
+	const int n = __popc(lm);
 	if (leader)
 		uniq[__popc(lm & ((1u << lane) - 1))] = x | (__popc(peers) << 16);
+	/* zero entries (value 0, count 0) up to a multiple of 4, so that a scan
+	   can read four at a time */
+	if (lane >= n && lane < ((n + 3) & ~3))
+		uniq[lane] = 0;
 	__syncwarp();
-	return __popc(lm);
+	return n;
 }
 
 /* Sets node 0 (a zero-error candidate) of a list. */
@@ -196,7 +201,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	}
 	const bool topNeg = HALF && top < 0;   /* signed compare rejects everything */
 
-	const int rowSize = HALF ? (1 << (2 * shift - 1)) : (1 << (2 * shift));
+	const int rowSize = 1 << (2 * shift);   /* byte tables; the half tables (shift 8) go by HalfAt */
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 	const bool pvar = HALF || pbits >= 0;
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
@@ -242,17 +247,22 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 			unsigned key = 0xFFFFFFFFu;
 			if (on)
 			{
-				unsigned s = 0;
-				for (int u = 0; u < nu; u++)
-				{
-					const int e = uniq[u];
+				/* four distinct values per step, their table reads in flight
+				   together (unsigned sums do not depend on the order) */
+				auto term = [&](int e) {
 					const int x = e & 0xFFFF;
 					unsigned v;
 					if (HALF)
-						v = (table[size_t(x) * rowSize + (cc >> 1)] >> ((cc & 1) << 2)) & 0xF;
+						v = HalfAt(table, x, cc & 0xFF, cc >> 8);
 					else
 						v = table[size_t(x) * rowSize + cc];
-					s += unsigned(e >> 16) * v * v;
+					return unsigned(e >> 16) * v * v;
+				};
+				unsigned s = 0;
+				for (int u = 0; u < nu; u += 4)
+				{
+					const int4 e4 = *reinterpret_cast<const int4*>(uniq + u);
+					s += (term(e4.x) + term(e4.y)) + (term(e4.z) + term(e4.w));
 				}
 				if (!HALF && s > 0xFFFF)
 					s = 0xFFFF;

@@ -10,7 +10,9 @@
  * replication; "shared" tables mark pairs with different p-bit parity as
  * 0xFF; "half" tables hold 4-bit nibbles clamped to 15; cut tables hold the
  * squared minimum over the row prefix [0, iH | 31].  Same contents as the
- * reference's InitLevels (src/Bc7Tables.cpp:497-777).
+ * reference's InitLevels (src/Bc7Tables.cpp:497-777); the half tables are
+ * indexed by endpoint-minus-value differences instead of by (x, c)
+ * (HalfAt), which gives the same entries from a 128 KB table.
  */
 #pragma once
 
@@ -18,38 +20,24 @@
 
 namespace nebc7 {
 
-__global__ void KBuildFull(uint8_t* out, int levels, int denoise, int clampNibble)
+__global__ void KBuildFull(uint8_t* out, int levels, int denoise)
 {
-	/* one thread per (x, c); nibble tables: one thread per (x, even c) */
+	/* one thread per (x, c) */
 	const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	const int per = clampNibble ? 0x8000 : 0x10000;
-	if (t >= uint64_t(256) * per)
+	if (t >= uint64_t(256) * 0x10000)
 		return;
-	const int x = int(t / per);
-	const int r = int(t % per);
+	const int x = int(t >> 16);
+	const int c = int(t & 0xFFFF);
 	const int* w = InterpWeights(levels == 4 ? 2 : (levels == 8 ? 3 : 4));
-	int res[2];
-	const int nc = clampNibble ? 2 : 1;
-	for (int j = 0; j < nc; j++)
+	const int cL = c & 0xFF, cH = c >> 8;
+	int best = 0x7FFF;
+	for (int k = 0; k < levels; k++)
 	{
-		const int c = clampNibble ? 2 * r + j : r;
-		const int cL = c & 0xFF, cH = c >> 8;
-		int best = 0x7FFF;
-		for (int k = 0; k < levels; k++)
-		{
-			int d = Interp(cL, cH, w[k]) - x;
-			d = d < 0 ? -d : d;
-			best = d < best ? d : best;
-		}
-		int q = denoise ? (best >> denoise) : (best > 127 ? 127 : best);
-		if (clampNibble && q > 15)
-			q = 15;
-		res[j] = q;
+		int d = Interp(cL, cH, w[k]) - x;
+		d = d < 0 ? -d : d;
+		best = d < best ? d : best;
 	}
-	if (clampNibble)
-		out[t] = uint8_t(res[0] | (res[1] << 4));
-	else
-		out[t] = uint8_t(res[0]);
+	out[t] = uint8_t(denoise ? (best >> denoise) : (best > 127 ? 127 : best));
 }
 
 __global__ void KReduce(const uint8_t* full, uint8_t* out, int bits, int shared)
@@ -84,17 +72,33 @@ __global__ void KCut(const uint8_t* table, uint16_t* tower, int bits)
 	tower[t] = uint16_t(cut * cut);
 }
 
-__global__ void KHalfFrom2(const uint8_t* d2v8, uint8_t* d2h)
+/* Half table by differences: byte a * 256 + bb holds the entries of
+   (a, b = 2 bb) and (a, 2 bb + 1), a = cH - x + 255, b = cL - x + 255; the
+   distance to level k is |(b - 255) + (((a - b) w_k + 32) >> 6)|, which is
+   Interp(cL, cH, w_k) - x.  Pairs (a, b) that no (x, cL, cH) reaches are
+   filled the same way and never read. */
+__global__ void KBuildHalfDiff(uint8_t* out, int levels, int denoise)
 {
-	const uint64_t t = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-	if (t >= uint64_t(256) * 0x8000)
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= 511 * 256)
 		return;
-	const int x = int(t / 0x8000), r = int(t % 0x8000);
-	int v0 = d2v8[size_t(x) * 0x10000 + 2 * r];
-	int v1 = d2v8[size_t(x) * 0x10000 + 2 * r + 1];
-	v0 = v0 > 15 ? 15 : v0;
-	v1 = v1 > 15 ? 15 : v1;
-	d2h[t] = uint8_t(v0 | (v1 << 4));
+	const int a = t >> 8;
+	const int* w = InterpWeights(levels == 4 ? 2 : 4);
+	int res[2];
+	for (int j = 0; j < 2; j++)
+	{
+		const int b = 2 * (t & 0xFF) + j;
+		int best = 0x7FFF;
+		for (int k = 0; k < levels; k++)
+		{
+			int d = (b - 255) + (((a - b) * w[k] + 32) >> 6);
+			d = d < 0 ? -d : d;
+			best = d < best ? d : best;
+		}
+		int q = denoise ? (best >> denoise) : (best > 127 ? 127 : best);
+		res[j] = q > 15 ? 15 : q;
+	}
+	out[t] = uint8_t(res[0] | (res[1] << 4));
 }
 
 } // namespace nebc7

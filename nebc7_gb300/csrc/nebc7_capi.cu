@@ -71,7 +71,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
 			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 128 * 2, size_t(256) * 32 * 2,
-			size_t(256) * 32768, size_t(256) * 32768,
+			size_t(511) * 256, size_t(511) * 256,
 		};
 		for (int i = 0; i < 14; i++)
 		{
@@ -89,14 +89,14 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		const int tb = 256;
 		auto grid = [&](uint64_t n) { return unsigned((n + tb - 1) / tb); };
 		/* 3-bit index tables (reference src/Bc7Tables.cpp:587-641) */
-		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d3v8, 8, denoise, 0);
+		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d3v8, 8, denoise);
 		KReduce<<<grid(uint64_t(256) * 16384), tb>>>(d3v8, (uint8_t*)D.mem[7], 7, 1);
 		KReduce<<<grid(uint64_t(256) * 4096), tb>>>(d3v8, (uint8_t*)D.mem[8], 6, 0);
 		KReduce<<<grid(uint64_t(256) * 1024), tb>>>(d3v8, (uint8_t*)D.mem[9], 5, 0);
 		KCut<<<grid(256 * 128), tb>>>((uint8_t*)D.mem[7], (uint16_t*)D.mem[10], 7);
 		KCut<<<grid(256 * 32), tb>>>((uint8_t*)D.mem[9], (uint16_t*)D.mem[11], 5);
 		/* 2-bit index tables (:643-692) */
-		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d2v8, 4, denoise, 0);
+		KBuildFull<<<grid(uint64_t(256) * 65536), tb>>>(d2v8, 4, denoise);
 		KReduce<<<grid(uint64_t(256) * 16384), tb>>>(d2v8, (uint8_t*)D.mem[1], 7, 0);
 		KReduce<<<grid(uint64_t(256) * 4096), tb>>>(d2v8, (uint8_t*)D.mem[2], 6, 0);
 		KReduce<<<grid(uint64_t(256) * 1024), tb>>>(d2v8, (uint8_t*)D.mem[3], 5, 0);
@@ -104,8 +104,8 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		KCut<<<grid(256 * 64), tb>>>((uint8_t*)D.mem[2], (uint16_t*)D.mem[5], 6);
 		KCut<<<grid(256 * 32), tb>>>((uint8_t*)D.mem[3], (uint16_t*)D.mem[6], 5);
 		/* 4-bit and 2-of-4-bit nibble tables (:694-776) */
-		KBuildFull<<<grid(uint64_t(256) * 32768), tb>>>((uint8_t*)D.mem[12], 16, denoise, 1);
-		KHalfFrom2<<<grid(uint64_t(256) * 32768), tb>>>(d2v8, (uint8_t*)D.mem[13]);
+		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[12], 16, denoise);
+		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[13], 4, denoise);
 		const cudaError_t e = cudaDeviceSynchronize();
 		cudaFree(d3v8);
 		if (e != cudaSuccess)
