@@ -51,12 +51,12 @@ template<int kD, int IB>
 __device__ __forceinline__ void PlaneAdd(int* dst, const int* src, const Area& ar, int np, int c, int col, int w, int lane)
 {
 	constexpr int L = 1 << IB;
-	const int* wk = InterpWeights(IB);
 	const int e0 = col & 0xFF, e1 = (col >> 8) & 0xFF;
+	/* entry e = lane + 32 m has level e & (L - 1) = lane & (L - 1) */
+	const int v = Interp(e0, e1, InterpWeights(IB)[lane & (L - 1)]);
 	for (int e = lane; e < np * L; e += 32)
 	{
-		const int i = e >> IB, k = e & (L - 1);
-		const int q = Q<kD>(int(ar.px[i][c]) - Interp(e0, e1, wk[k]));
+		const int q = Q<kD>(int(ar.px[e >> IB][c]) - v);
 		dst[e] = (src ? src[e] : 0) + w * q * q;
 	}
 	__syncwarp();
@@ -251,12 +251,16 @@ __device__ NEBC7_SHARED int TryVariants3(const Area& ar, const AreaInfo& ai, con
 			const int e2 = __shfl_sync(kFull, pairGR, i2);
 			if (e2 + min3 >= water)
 				continue;
-			PlaneAdd<kD, IB>(pGR, pG, ar, np, 2, col2, P.wR, lane);
 			const bool valid = lane < n3;
 			const int brk = valid ? e3base + e2 : kBig;
 			const int skip = valid ? memGB + min2 : kBig;
+			const bool eval = valid && brk < water && skip < water;
+			/* no lane evaluates: the replay accepts nothing, the plane is not needed */
+			if (!__any_sync(kFull, eval))
+				continue;
+			PlaneAdd<kD, IB>(pGR, pG, ar, np, 2, col2, P.wR, lane);
 			int err = kBig;
-			if (valid && brk < water && skip < water)
+			if (eval)
 				err = PlaneError<kD, IB>(pGR, ar, np, 3, col3, P.wB, water);
 			const int jl = ReplayInner(valid, brk, skip, err, water, lane);
 			if (jl >= 0)
@@ -687,13 +691,17 @@ __device__ __forceinline__ int TryVariants4Body(const Area& ar, const AreaInfo& 
 				const int e2 = __shfl_sync(kFull, pairAGR, i2);
 				if (e2 + min3 >= water)
 					continue;
-				PlaneAdd<kD, IB>(pAGR, pAG, ar, np, 2, c2, P.wR, lane);
-				const Ep base012 = EpSetCh(base01, 2, c2);
 				const bool valid = lane < n3;
 				const int brk = valid ? e3base + e2 : kBig;
 				const int skip = valid ? memAGB + min2 : kBig;
+				const bool eval = valid && brk < water && skip < water;
+				/* no lane evaluates: the replay accepts nothing, the plane is not needed */
+				if (!__any_sync(kFull, eval))
+					continue;
+				PlaneAdd<kD, IB>(pAGR, pAG, ar, np, 2, c2, P.wR, lane);
+				const Ep base012 = EpSetCh(base01, 2, c2);
 				int err = kBig;
-				if (valid && brk < water && skip < water)
+				if (eval)
 					err = PlaneError<kD, IB>(pAGR, ar, np, 3, col3, P.wB, water - ea) + ea;
 				const int jl = ReplayInner(valid, brk, skip, err, water, lane);
 				if (jl >= 0)
