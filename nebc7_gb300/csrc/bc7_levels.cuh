@@ -207,9 +207,13 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
 	const int pL = reverse ? (pbits >> 8) : (pbits & 1);
 
+	/* list: the maxSize smallest keys so far, lane j the j-th; thr: its last
+	   key (all ones until the list is full), which changes only on a merge.
+	   The number of kept candidates matters only up to maxSize, which is the
+	   number of filled list entries, and a list whose last key has error 0
+	   means maxSize zero-error candidates were found. */
 	unsigned list = 0xFFFFFFFFu;
-	int stored = 0;
-	int zeros = 0;
+	unsigned thr = 0xFFFFFFFFu;
 	const int rowStep = pvar ? 2 : 1;
 	/* hL - cH = LH for every row: when LH is below one chunk, only the first
 	   chunk of a row can be on and a batch takes two rows (lanes 16..31 the
@@ -270,20 +274,20 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 				if (keep)
 					key = (s << 16) | unsigned(cc);
 			}
-			const unsigned ballot = __ballot_sync(kFull, key != 0xFFFFFFFFu);
-			stored += __popc(ballot);
-			zeros += __popc(__ballot_sync(kFull, key != 0xFFFFFFFFu && (key >> 16) == 0));
-			const unsigned thr = __shfl_sync(kFull, list, maxSize - 1);
 			if (__any_sync(kFull, key < thr))
+			{
 				list = MergeTop(list, key < thr ? key : 0xFFFFFFFFu, lane, maxSize);
+				thr = __shfl_sync(kFull, list, maxSize - 1);
+			}
 		}
 		/* maxSize zero-error candidates found: later ones (larger c) cannot enter */
-		if (zeros >= maxSize)
+		if (thr < 0x10000u)
 			break;
 	}
+	const int stored = __popc(__ballot_sync(kFull, list != 0xFFFFFFFFu));
 	if (stored)
 	{
-		res.count = min(stored, maxSize);
+		res.count = stored;
 		const unsigned k0 = __shfl_sync(kFull, list, 0);
 		res.minErr = int(k0 >> 16) * weight;
 		if (lane < res.count)
