@@ -55,6 +55,7 @@ struct Job
 	BlockResult* results;    /* optional, one per queue position */
 	int* counter;            /* work queue head, zero before launch */
 	int* status;             /* set non-zero on an internal limit */
+	const int* order;        /* optional: queue position -> block (`single` only) */
 };
 
 /* kD template value of the kernel that reads kDenoise from each texture */
@@ -248,6 +249,8 @@ template<int kD, bool NORMAL>
 __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T0,
 	const LevelTables& T1, int k, int lane)
 {
+	if (job.order)
+		k = job.order[k];
 	int t = 0;
 	if (job.tex)
 	{

@@ -147,4 +147,78 @@ __global__ void KPartitionMap(const uint8_t* blocks, uint8_t* out, int n)
 	reinterpret_cast<uint4*>(out)[k] = make_uint4(unsigned(d0), unsigned(d0 >> 32), unsigned(d1), unsigned(d1 >> 32));
 }
 
+/* Hot-first block order of one texture.  The blocks of a texture are
+   independent and each writes its own slots, so the order in which a launch
+   takes them changes nothing in its output; taking the blocks with the
+   widest pixel ranges (the long searches) first leaves short ones for the
+   end of the launch.  KBlockBuckets: bucket 255 - min(255, range / 4) per
+   block, range = sum over B, G, R, A of max - min over its 16 pixels, and a
+   histogram of the buckets (zero before the launch). */
+__global__ void KBlockBuckets(const uint8_t* bgra, long long stride, int blocksW, int nblocks, uint8_t* bucket, int* hist)
+{
+	__shared__ int h[256];
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		h[i] = 0;
+	__syncthreads();
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k < nblocks)
+	{
+		const int bx = k % blocksW, by = k / blocksW;
+		const uint8_t* p = bgra + (long long)by * 4 * stride + (long long)bx * 16;
+		unsigned lo = 0xFFFFFFFFu, hi = 0;
+		for (int r = 0; r < 4; r++)
+			for (int x = 0; x < 4; x++)
+			{
+				const unsigned v = *reinterpret_cast<const uint32_t*>(p + r * stride + x * 4);
+				lo = __vminu4(lo, v);
+				hi = __vmaxu4(hi, v);
+			}
+		const unsigned d = __vsubus4(hi, lo);
+		const int range = int(d & 0xFF) + int((d >> 8) & 0xFF) + int((d >> 16) & 0xFF) + int(d >> 24);
+		const int b = 255 - min(255, range >> 2);
+		bucket[k] = uint8_t(b);
+		atomicAdd(&h[b], 1);
+	}
+	__syncthreads();
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		if (h[i])
+			atomicAdd(&hist[i], h[i]);
+}
+
+/* Counting-sort scatter: order[] lists the blocks bucket by bucket (any
+   order inside a bucket); cursor[] is zero before the launch.  256 threads
+   per CTA. */
+__global__ void KBlockOrder(const uint8_t* bucket, int nblocks, const int* hist, int* cursor, int* order)
+{
+	__shared__ int base[256];
+	if (threadIdx.x < 32)
+	{
+		/* exclusive scan of the 256 counts: 8 per lane, then across lanes */
+		const int lane = threadIdx.x;
+		int c[8], run = 0;
+		for (int j = 0; j < 8; j++)
+		{
+			c[j] = run;
+			run += hist[lane * 8 + j];
+		}
+		int incl = run;
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			const int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+			if (lane >= o)
+				incl += v;
+		}
+		const int excl = incl - run;
+		for (int j = 0; j < 8; j++)
+			base[lane * 8 + j] = excl + c[j];
+	}
+	__syncthreads();
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k < nblocks)
+	{
+		const int b = bucket[k];
+		order[base[b] + atomicAdd(&cursor[b], 1)] = k;
+	}
+}
+
 } // namespace nebc7

@@ -266,14 +266,72 @@ Job SingleJob(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long 
 	job.results = results;
 	job.counter = counter;
 	job.status = status;
+	job.order = nullptr;
 	return job;
 }
 
-/* Scratch of one encode: the work-queue head and status word, the reduced
-   sums and, when sums are wanted, one BlockResult per block. */
-size_t EncodeScratchBytes(int nblocks, bool wantSums)
+/* Scratch of one encode, in 256-byte aligned pieces: the work-queue head,
+   status word and reduced sums (256 bytes); the block-order histogram and
+   cursors (2 KB); the block order (an int per block) and buckets (a byte per
+   block); one BlockResult per block when sums are wanted.  The first
+   kScratchZeroed bytes must be zero before a launch. */
+constexpr size_t kScratchZeroed = 256 + 2048;
+
+constexpr size_t ScratchAlign(size_t v) { return (v + 255) & ~size_t(255); }
+
+constexpr size_t EncodeScratchBytes(int nblocks, bool wantSums)
 {
-	return 256 + (wantSums ? size_t(nblocks) * sizeof(BlockResult) : 0) + 64;
+	return kScratchZeroed + ScratchAlign(size_t(nblocks) * 4) + ScratchAlign(size_t(nblocks)) +
+		(wantSums ? size_t(nblocks) * sizeof(BlockResult) : 0) + 64;
+}
+
+/* Pieces of a scratch laid out by EncodeScratchBytes. */
+struct EncodeScratch
+{
+	int* counter;
+	int* status;
+	long long* sums;
+	double* ssums;
+	int* hist;
+	int* cursor;
+	int* order;
+	uint8_t* bucket;
+	BlockResult* results;
+};
+
+EncodeScratch SplitScratch(uint8_t* scratch, int nblocks, bool wantSums)
+{
+	EncodeScratch e;
+	e.counter = (int*)scratch;
+	e.status = e.counter + 1;
+	e.sums = (long long*)(scratch + 64);
+	e.ssums = (double*)(scratch + 128);
+	e.hist = (int*)(scratch + 256);
+	e.cursor = e.hist + 256;
+	e.order = (int*)(scratch + kScratchZeroed);
+	e.bucket = scratch + kScratchZeroed + ScratchAlign(size_t(nblocks) * 4);
+	e.results = wantSums ? (BlockResult*)(e.bucket + ScratchAlign(size_t(nblocks))) : nullptr;
+	return e;
+}
+
+/* The refining variants take a texture's blocks widest pixel range first
+   (KBlockBuckets); the draft-only ones, whose blocks cost about the same,
+   in raster order. */
+bool OrdersBlocks(const nebc7_settings& s)
+{
+	return s.doNormal && s.doDraft != 2;
+}
+
+/* Enqueues the block order of one texture into e.order (e's zeroed head
+   must already be zero on the stream). */
+cudaError_t EnqueueBlockOrder(const uint8_t* bgra, long long stride, int blocksW, int nblocks, const EncodeScratch& e,
+	cudaStream_t stream)
+{
+	const int tb = 256;
+	const int grid = (nblocks + tb - 1) / tb;
+	KBlockBuckets<<<grid, tb, 0, stream>>>(bgra, stride, blocksW, nblocks, e.bucket, e.hist);
+	KBlockOrder<<<grid, tb, 0, stream>>>(e.bucket, nblocks, e.hist, e.cursor, e.order);
+	return cudaGetLastError();
 }
 
 /* Enqueues one encode.  `scratchIn` (EncodeScratchBytes bytes, 256-byte
@@ -300,14 +358,19 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 	uint8_t* scratch = scratchIn;
 	if (!scratch && cudaMallocAsync((void**)&scratch, EncodeScratchBytes(nblocks, wantSums), stream) != cudaSuccess)
 		return SetError(NEBC7_ENOMEM);
-	int* counter = (int*)scratch;
-	int* status = counter + 1;
-	long long* sums = (long long*)(scratch + 64);
-	double* ssums = (double*)(scratch + 128);
-	BlockResult* results = wantSums ? (BlockResult*)(scratch + 256) : nullptr;
-	CK(cudaMemsetAsync(scratch, 0, 256, stream));
+	const EncodeScratch e = SplitScratch(scratch, nblocks, wantSums);
+	int* status = e.status;
+	long long* sums = e.sums;
+	double* ssums = e.ssums;
+	BlockResult* results = e.results;
+	CK(cudaMemsetAsync(scratch, 0, kScratchZeroed, stream));
 
-	const Job job = SingleJob(dst, bgra, mask, stride, blocksW, nblocks, s, results, counter, status);
+	Job job = SingleJob(dst, bgra, mask, stride, blocksW, nblocks, s, results, e.counter, status);
+	if (OrdersBlocks(s))
+	{
+		CK(EnqueueBlockOrder(bgra, stride, blocksW, nblocks, e, stream));
+		job.order = e.order;
+	}
 	const int grid = GridFor(nblocks, s);
 	if (grid <= 0)
 	{
@@ -640,6 +703,7 @@ int EnqueueSchedule(nebc7_batch* b, int which, cudaStream_t st)
 		job.results = b->results + G.queueBase;
 		job.counter = b->counters + 2 * g;
 		job.status = b->counters + 2 * g + 1;
+		job.order = nullptr;
 		job.single = S.table[G.firstTex];
 		const cudaStream_t gs = g == 0 ? st : b->side[g - 1];
 		CK(kVariants[G.slot].launch(G.grid, gs, job, *b->T[0], *b->T[1]));
@@ -896,6 +960,7 @@ int LaunchServerBatch(nebc7_server* sv, ServerSlot& slot, std::vector<int64_t>& 
 	job.results = nullptr;
 	job.counter = slot.dCounter;
 	job.status = slot.dCounter + 1;
+	job.order = nullptr;
 	job.single = slot.hTable[0];
 	const int grid = GridForSlot(total, kVariantMixed);
 	if (grid <= 0)
@@ -1115,9 +1180,10 @@ void FreeServer(nebc7_server* sv)
 /* Largest texture nebc7_encode_device_noalloc accepts: 65536 blocks
    (1024x1024 pixels).  Its scratch lives in this fixed device array instead
    of coming from an allocator: 256 bytes for the work-queue head and the
-   status word, then one BlockResult per block for the error / SSIM sums. */
+   status word, the block order, then one BlockResult per block for the
+   error / SSIM sums (the layout of EncodeScratchBytes). */
 constexpr int kNoAllocMaxBlocks = 65536;
-constexpr size_t kNoAllocScratchBytes = 256 + size_t(kNoAllocMaxBlocks) * sizeof(BlockResult);
+constexpr size_t kNoAllocScratchBytes = EncodeScratchBytes(kNoAllocMaxBlocks, true);
 static __device__ __align__(256) unsigned char gNoAllocScratch[kNoAllocScratchBytes];
 
 namespace {
@@ -1182,10 +1248,15 @@ int nebc7_encode_device_noalloc(uint8_t* d_dst, const uint8_t* d_bgra, const uin
 		return SetError(NEBC7_ECUDA);
 
 	const cudaStream_t st = (cudaStream_t)stream;
-	/* the queue head and status word must start at zero */
-	CK(cudaMemsetAsync(scratch, 0, 256, st));
-	const Job job = SingleJob(d_dst, d_bgra, d_mask, stride, w / 4, int(nb), *settings,
-		d_sums ? (BlockResult*)(scratch + 256) : nullptr, (int*)scratch, (int*)scratch + 1);
+	/* the queue head, status word and block-order counts must start at zero */
+	CK(cudaMemsetAsync(scratch, 0, kScratchZeroed, st));
+	const EncodeScratch e = SplitScratch(scratch, int(nb), d_sums != nullptr);
+	Job job = SingleJob(d_dst, d_bgra, d_mask, stride, w / 4, int(nb), *settings, e.results, e.counter, e.status);
+	if (OrdersBlocks(*settings))
+	{
+		CK(EnqueueBlockOrder(d_bgra, stride, w / 4, int(nb), e, st));
+		job.order = e.order;
+	}
 	CK(kVariants[VariantSlot(*settings)].launch(grid, st, job, *T, *T));
 	if (d_sums)
 	{
