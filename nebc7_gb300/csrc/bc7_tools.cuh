@@ -187,7 +187,7 @@ __global__ void KBlockBuckets(const uint8_t* bgra, long long stride, int blocksW
 
 /* Counting-sort scatter: order[] lists the blocks bucket by bucket (any
    order inside a bucket); cursor[] is zero before the launch.  256 threads
-   per CTA. */
+   per CTA, every thread of a warp reaching the warp-wide steps. */
 __global__ void KBlockOrder(const uint8_t* bucket, int nblocks, const int* hist, int* cursor, int* order)
 {
 	__shared__ int base[256];
@@ -213,12 +213,19 @@ __global__ void KBlockOrder(const uint8_t* bucket, int nblocks, const int* hist,
 			base[lane * 8 + j] = excl + c[j];
 	}
 	__syncthreads();
+	/* one atomic per distinct bucket of a warp (most blocks of a texture
+	   share a few buckets) */
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	const int lane = threadIdx.x & 31;
+	const int b = k < nblocks ? int(bucket[k]) : 256 + lane;
+	const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+	const int leader = __ffs(peers) - 1;
+	int pos = 0;
+	if (lane == leader && b < 256)
+		pos = atomicAdd(&cursor[b], __popc(peers));
+	pos = __shfl_sync(0xFFFFFFFFu, pos, leader);
 	if (k < nblocks)
-	{
-		const int b = bucket[k];
-		order[base[b] + atomicAdd(&cursor[b], 1)] = k;
-	}
+		order[base[b] + pos + __popc(peers & ((1u << lane) - 1))] = k;
 }
 
 } // namespace nebc7
