@@ -779,7 +779,7 @@ __device__ __forceinline__ int TransparentError2(const LevelTables& T, const Par
 	if (e)
 	{
 		e *= P.wA;
-		const int v = T.d2v8[alpha & 0xFFFF];
+		const int v = DiffAt(T.d2v8, 0, alpha & 0xFF, (alpha >> 8) & 0xFF);
 		e *= v * v;
 	}
 	return e;

@@ -72,7 +72,7 @@ static __constant__ int c_rot5[4] = { 0, 2, 1, 3 };
    and contents as described in the table builder). */
 struct LevelTables
 {
-	const uint8_t* d2v8;   /* [256][256*256] */
+	const uint8_t* d2v8;   /* [511][512] bytes, by differences (DiffAt) */
 	const uint8_t* d2v7;   /* [256][128*128] */
 	const uint8_t* d2v6;   /* [256][64*64]   */
 	const uint8_t* d2v5;   /* [256][32*32]   */
@@ -128,6 +128,15 @@ __device__ __forceinline__ int HalfAt(const uint8_t* table, int x, int cL, int c
 {
 	const int a = cH - x + 255, b = cL - x + 255;
 	return (table[a * 256 + (b >> 1)] >> ((b & 1) << 2)) & 0xF;
+}
+
+/* Entry (x, cL, cH) of the 8-bit-endpoint byte table of 2-bit indices, the
+   same function of cH - x and cL - x as HalfAt's, unclamped: rows of 512
+   bytes (511 used) by cH - x + 255, columns by cL - x + 255, 256 KB for every
+   x instead of 256 rows of 64 KB. */
+__device__ __forceinline__ int DiffAt(const uint8_t* table, int x, int cL, int cH)
+{
+	return table[((cH - x + 255) << 9) + (cL - x + 255)];
 }
 
 __device__ __forceinline__ const int* InterpWeights(int bits)

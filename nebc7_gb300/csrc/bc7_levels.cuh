@@ -201,7 +201,10 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	}
 	const bool topNeg = HALF && top < 0;   /* signed compare rejects everything */
 
-	const int rowSize = 1 << (2 * shift);   /* byte tables; the half tables (shift 8) go by HalfAt */
+	/* byte tables by (x, c); with 8-bit endpoints (shift 8) the byte table
+	   goes by DiffAt and the half tables by HalfAt */
+	const int rowSize = 1 << (2 * shift);
+	const bool diff = shift == 8;
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 	const bool pvar = HALF || pbits >= 0;
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
@@ -258,6 +261,8 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 					unsigned v;
 					if (HALF)
 						v = HalfAt(table, x, cc & 0xFF, cc >> 8);
+					else if (diff)
+						v = DiffAt(table, x, cc & 0xFF, cc >> 8);
 					else
 						v = table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
@@ -331,6 +336,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 		top = 0xFFFF;
 	const unsigned top16 = unsigned(top) & 0xFFFF;
 	const int rowSize = 1 << (2 * shift);
+	const bool diff = shift == 8;   /* the 8-bit byte table goes by DiffAt */
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
 	unsigned best = 0xFFFFFFFFu;
@@ -352,12 +358,16 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 				break;
 			if (chunkOn && ((mask >> (2 * j)) & 1))
 			{
+				auto term = [&](int e) {
+					const int x = e & 0xFFFF;
+					const unsigned v = diff ? DiffAt(table, x, cc & 0xFF, cc >> 8) : table[size_t(x) * rowSize + cc];
+					return unsigned(e >> 16) * v * v;
+				};
 				unsigned s = 0;
-				for (int u = 0; u < nu; u++)
+				for (int u = 0; u < nu; u += 4)
 				{
-					const int e = uniq[u];
-					const unsigned v = table[size_t(e & 0xFFFF) * rowSize + cc];
-					s += unsigned(e >> 16) * v * v;
+					const int4 e4 = *reinterpret_cast<const int4*>(uniq + u);
+					s += (term(e4.x) + term(e4.y)) + (term(e4.z) + term(e4.w));
 				}
 				if (s > 0xFFFF)
 					s = 0xFFFF;
@@ -407,6 +417,7 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 	if (top > 0xFFFF)
 		top = 0xFFFF;
 	const int rowSize = 1 << (2 * bits);
+	const bool diff = bits == 8;   /* the 8-bit byte table goes by DiffAt */
 	const int towerSize = 1 << bits;
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
@@ -418,11 +429,12 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 		unsigned rowLb = 0xFFFF;
 		if (iHl < win.HH)
 		{
+			auto cut = [&](int e) { return unsigned(e >> 16) * tower[size_t(e & 0xFFFF) * towerSize + iHl]; };
 			unsigned s = 0;
-			for (int u = 0; u < nu; u++)
+			for (int u = 0; u < nu; u += 4)
 			{
-				const int e = uniq[u];
-				s += unsigned(e >> 16) * tower[size_t(e & 0xFFFF) * towerSize + iHl];
+				const int4 e4 = *reinterpret_cast<const int4*>(uniq + u);
+				s += (cut(e4.x) + cut(e4.y)) + (cut(e4.z) + cut(e4.w));
 			}
 			rowLb = s > 0xFFFF ? 0xFFFF : s;
 		}
@@ -437,12 +449,18 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 			unsigned rowBest = 0xFFFF;
 			for (int iL = cH, hL = min(win.LH, iH) + cH; iL <= hL; iL += 32)
 			{
+				/* cc = iL + lane stays in row iH (iL <= hL, iL - cH a multiple of 32) */
+				const int cc = iL + lane;
+				auto term = [&](int e) {
+					const int x = e & 0xFFFF;
+					const unsigned v = diff ? DiffAt(table, x, cc & 0xFF, cc >> 8) : table[size_t(x) * rowSize + cc];
+					return unsigned(e >> 16) * v * v;
+				};
 				unsigned s = 0;
-				for (int u = 0; u < nu; u++)
+				for (int u = 0; u < nu; u += 4)
 				{
-					const int e = uniq[u];
-					const unsigned v = table[size_t(e & 0xFFFF) * rowSize + iL + lane];
-					s += unsigned(e >> 16) * v * v;
+					const int4 e4 = *reinterpret_cast<const int4*>(uniq + u);
+					s += (term(e4.x) + term(e4.y)) + (term(e4.z) + term(e4.w));
 				}
 				if (s > 0xFFFF)
 					s = 0xFFFF;

@@ -10,9 +10,10 @@
  * replication; "shared" tables mark pairs with different p-bit parity as
  * 0xFF; "half" tables hold 4-bit nibbles clamped to 15; cut tables hold the
  * squared minimum over the row prefix [0, iH | 31].  Same contents as the
- * reference's InitLevels (src/Bc7Tables.cpp:497-777); the half tables are
- * indexed by endpoint-minus-value differences instead of by (x, c)
- * (HalfAt), which gives the same entries from a 128 KB table.
+ * reference's InitLevels (src/Bc7Tables.cpp:497-777); the tables with 8-bit
+ * endpoints (the 2-bit byte table and the two half tables) are indexed by
+ * endpoint-minus-value differences instead of by (x, c) (DiffAt, HalfAt),
+ * which gives the same entries from 256 KB and 128 KB tables.
  */
 #pragma once
 
@@ -99,6 +100,31 @@ __global__ void KBuildHalfDiff(uint8_t* out, int levels, int denoise)
 		res[j] = q > 15 ? 15 : q;
 	}
 	out[t] = uint8_t(res[0] | (res[1] << 4));
+}
+
+/* Byte table by differences (DiffAt): byte (a << 9) + b holds the entry of
+   a = cH - x + 255, b = cL - x + 255, quantised like KBuildFull; column 511
+   is padding. */
+__global__ void KBuildByteDiff(uint8_t* out, int levels, int denoise)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= 511 * 512)
+		return;
+	const int a = t >> 9, b = t & 511;
+	if (b == 511)
+	{
+		out[t] = 0;
+		return;
+	}
+	const int* w = InterpWeights(levels == 4 ? 2 : (levels == 8 ? 3 : 4));
+	int best = 0x7FFF;
+	for (int k = 0; k < levels; k++)
+	{
+		int d = (b - 255) + (((a - b) * w[k] + 32) >> 6);
+		d = d < 0 ? -d : d;
+		best = d < best ? d : best;
+	}
+	out[t] = uint8_t(denoise ? (best >> denoise) : (best > 127 ? 127 : best));
 }
 
 } // namespace nebc7

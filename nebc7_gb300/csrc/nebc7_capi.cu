@@ -67,7 +67,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 	if (!D.built)
 	{
 		const size_t sizes[23] = {
-			size_t(256) * 65536, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
+			size_t(511) * 512, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
 			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 128 * 2, size_t(256) * 32 * 2,
@@ -82,10 +82,16 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 				return SetError(NEBC7_ENOMEM);
 			}
 		}
+		/* per-x full tables, only to build the reduced and cut tables from */
 		uint8_t* d3v8 = nullptr;
+		uint8_t* d2v8 = nullptr;
 		if (cudaMalloc(&d3v8, size_t(256) * 65536) != cudaSuccess)
 			return SetError(NEBC7_ENOMEM);
-		uint8_t* d2v8 = (uint8_t*)D.mem[0];
+		if (cudaMalloc(&d2v8, size_t(256) * 65536) != cudaSuccess)
+		{
+			cudaFree(d3v8);
+			return SetError(NEBC7_ENOMEM);
+		}
 		const int tb = 256;
 		auto grid = [&](uint64_t n) { return unsigned((n + tb - 1) / tb); };
 		/* 3-bit index tables (reference src/Bc7Tables.cpp:587-641) */
@@ -106,8 +112,10 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		/* 4-bit and 2-of-4-bit nibble tables (:694-776) */
 		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[12], 16, denoise);
 		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[13], 4, denoise);
+		KBuildByteDiff<<<grid(511 * 512), tb>>>((uint8_t*)D.mem[0], 4, denoise);
 		const cudaError_t e = cudaDeviceSynchronize();
 		cudaFree(d3v8);
+		cudaFree(d2v8);
 		if (e != cudaSuccess)
 			return SetError(NEBC7_ECUDA);
 		LevelTables& t = D.t;
