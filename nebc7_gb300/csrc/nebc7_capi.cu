@@ -66,30 +66,38 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 	DeviceTables& D = gTables[dev][denoise];
 	if (!D.built)
 	{
-		const size_t sizes[23] = {
+		const size_t sizes[14] = {
 			size_t(511) * 512, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
 			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 			size_t(256) * 128 * 2, size_t(256) * 32 * 2,
 			size_t(511) * 256, size_t(511) * 256,
 		};
+		/* per-x full tables, only to build the reduced and cut tables from */
+		uint8_t* d3v8 = nullptr;
+		uint8_t* d2v8 = nullptr;
+		/* a failed build leaves nothing allocated, so a later call starts over */
+		auto release = [&]() {
+			for (void*& m : D.mem)
+			{
+				cudaFree(m);
+				m = nullptr;
+			}
+			cudaFree(d3v8);
+			cudaFree(d2v8);
+		};
 		for (int i = 0; i < 14; i++)
 		{
 			if (cudaMalloc(&D.mem[i], sizes[i]) != cudaSuccess)
 			{
-				for (int j = 0; j < i; j++)
-					cudaFree(D.mem[j]);
+				release();
 				return SetError(NEBC7_ENOMEM);
 			}
 		}
-		/* per-x full tables, only to build the reduced and cut tables from */
-		uint8_t* d3v8 = nullptr;
-		uint8_t* d2v8 = nullptr;
-		if (cudaMalloc(&d3v8, size_t(256) * 65536) != cudaSuccess)
-			return SetError(NEBC7_ENOMEM);
-		if (cudaMalloc(&d2v8, size_t(256) * 65536) != cudaSuccess)
+		if (cudaMalloc(&d3v8, size_t(256) * 65536) != cudaSuccess ||
+			cudaMalloc(&d2v8, size_t(256) * 65536) != cudaSuccess)
 		{
-			cudaFree(d3v8);
+			release();
 			return SetError(NEBC7_ENOMEM);
 		}
 		const int tb = 256;
@@ -116,8 +124,12 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		const cudaError_t e = cudaDeviceSynchronize();
 		cudaFree(d3v8);
 		cudaFree(d2v8);
+		d3v8 = d2v8 = nullptr;
 		if (e != cudaSuccess)
+		{
+			release();
 			return SetError(NEBC7_ECUDA);
+		}
 		LevelTables& t = D.t;
 		t.d2v8 = (const uint8_t*)D.mem[0];
 		t.d2v7 = (const uint8_t*)D.mem[1];
