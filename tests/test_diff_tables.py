@@ -14,7 +14,8 @@ reference's entry.
 import numpy as np
 import pytest
 
-WEIGHTS = {4: (0, 21, 43, 64), 16: (0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64)}
+WEIGHTS = {4: (0, 21, 43, 64), 8: (0, 9, 18, 27, 37, 46, 55, 64),
+           16: (0, 4, 9, 13, 17, 21, 26, 30, 34, 38, 43, 47, 51, 55, 60, 64)}
 
 
 def _quantise(d, denoise, clamp):
@@ -73,3 +74,46 @@ def test_byte_table_row_layout():
     x, cL, cH = 17, 200, 3
     a, b = cH - x + 255, cL - x + 255
     assert flat[(a << 9) + b] == _reference_rows(4, 0, clamp=False)[x][cH, cL]
+
+
+# (table id in the port, index levels, endpoint bits, shared p-bit, nibbles)
+PORT_TABLES = {
+    "d2v8": (0, 4, 8, False, False), "d2v7": (1, 4, 7, False, False), "d2v6": (2, 4, 6, False, False),
+    "d2v5": (3, 4, 5, False, False), "d3v7s": (7, 8, 7, True, False), "d3v6": (8, 8, 6, False, False),
+    "d3v5": (9, 8, 5, False, False), "d4h": (12, 16, 8, False, True), "d2h": (13, 4, 8, False, True),
+}
+
+
+def _port_table(denoise, tid):
+    import ctypes
+    from oracle.pyoracle import Port
+    p = Port()
+    n = ctypes.c_int()
+    ptr = p.lib.nebc7_oracle_table(denoise, tid, ctypes.byref(n))
+    return np.frombuffer(ctypes.string_at(ptr, n.value), np.uint8)
+
+
+@pytest.mark.parametrize("denoise", [0, 1])
+@pytest.mark.parametrize("name", sorted(PORT_TABLES))
+def test_reference_tables_from_difference_tables(denoise, name):
+    """Every byte and nibble table of the reference (as the port holds it,
+    pinned to the reference build) is the difference table of its index
+    width read at the bit-replicated endpoints, with a shared table's pairs
+    of different parity marked 0xFF."""
+    tid, levels, bits, shared, nibbles = PORT_TABLES[name]
+    diff = _difference_table(levels, denoise, clamp=nibbles)
+    n = 1 << bits
+    ref = _port_table(denoise, tid)
+    if nibbles:
+        ref = np.stack([ref & 0xF, ref >> 4], axis=-1).reshape(256, n * n)
+    else:
+        ref = ref.reshape(256, n * n)
+    q = np.arange(n)
+    e = (q << (8 - bits)) + ((q << (8 - bits)) >> bits)
+    qH, qL = np.meshgrid(q, q, indexing="ij")
+    eH, eL = e[qH], e[qL]
+    marked = shared & (((qH ^ qL) & 1) == 1)
+    xs = range(256) if n <= 128 else range(0, 256, 5)
+    for x in xs:
+        got = np.where(marked, 0xFF, diff[eH - x + 255, eL - x + 255]).reshape(-1)
+        assert np.array_equal(got, ref[x]), f"{name} x={x}"
