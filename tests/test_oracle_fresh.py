@@ -59,6 +59,8 @@ IMAGES = [
     ("alpha_blobs", 32, 24, 32, "/noflip /slow", 1, 9),
     ("photo_like", 42, 21, 33, "/nomask /noflip", 0, 0),
     ("gradient_noise", 37, 29, 34, "/noflip /draft", 1, 9),
+    ("gradient_noise", 16, 12, 35, "/nomask /noflip /data", 1, 9),
+    ("alpha_blobs", 28, 20, 36, "/noflip /retina", 0, 0),
 ]
 
 
