@@ -135,6 +135,20 @@ class NvmlSampler:
                 "reasons": reasons, "samples": len(self.samples), "source": "nvml"}
 
 
+def issue_roofline(prof, kernel_ms, sm_mhz, n_sms):
+    """Warp-instruction issue rate of the encode call against the SMs' issue
+    peak: 4 schedulers per SM, one warp instruction each per cycle, at the SM
+    clock sampled during the timed region.  The instructions per launch come
+    from the committed ncu capture of the same workload.  None without that
+    capture or without a clock sample."""
+    if not prof or not prof.get("warp_inst_per_launch") or not sm_mhz or not kernel_ms or kernel_ms <= 0:
+        return None
+    achieved = prof["warp_inst_per_launch"] / (kernel_ms / 1e3) / 1e9
+    peak = 4.0 * n_sms * sm_mhz * 1e6 / 1e9
+    return {"achieved": achieved, "peak": peak, "unit": "G warp-inst/s", "frac": achieved / peak,
+            "warp_inst_per_launch": prof["warp_inst_per_launch"], "source": "profiles/" + prof["summary"]}
+
+
 def cpu_rate(padded, mask, o, d, s, budget_s=12.0, threads=None):
     """Oracle port on the host cores over a bounded band of block rows."""
     from oracle.pyoracle import Port
@@ -373,7 +387,7 @@ def run_ours(args, rank, world, local):
     achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
     # per-launch DRAM traffic and issue utilisation of the encode kernel, from the
     # committed ncu capture of this workload (null when there is none)
-    traffic, issue = None, None
+    traffic, issue, prof = None, None, None
     tf = ROOT / "profiles" / "kencode_ncu.json"
     if tf.exists():
         prof = json.loads(tf.read_text()).get(args.workload)
@@ -397,6 +411,8 @@ def run_ours(args, rank, world, local):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "peak_source": peak_src, "kernel_ms": kernel_ms,
                          "algorithmic_bytes_per_block": algo_bytes // nblocks, "issue_ncu": issue,
+                         "issue": issue_roofline(prof, kernel_ms, clocks.summary()["sm_mhz"],
+                                                 torch.cuda.get_device_properties(dev).multi_processor_count),
                          "note": "integer-issue and latency bound search; HBM bytes are the algorithmic "
                                  "input/output bytes, of measured peak; kernel_ms covers the encode call "
                                  "(block order and KEncode)"},
