@@ -135,18 +135,78 @@ class NvmlSampler:
                 "reasons": reasons, "samples": len(self.samples), "source": "nvml"}
 
 
+def source_sha():
+    """SHA-256 (16 hex digits) of the CUDA sources the library is built from;
+    an ncu capture records the value of the build it measured."""
+    h = hashlib.sha256()
+    for f in sorted((ROOT / "nebc7_gb300" / "csrc").iterdir()):
+        if f.suffix in (".cu", ".cuh"):
+            h.update(f.name.encode() + b"\0" + f.read_bytes())
+    return h.hexdigest()[:16]
+
+
+def current_capture(prof):
+    """The committed ncu capture of a workload, only if it measured the
+    CUDA sources this bench runs (else None)."""
+    if not prof or prof.get("source_sha") != source_sha():
+        return None
+    return prof
+
+
 def issue_roofline(prof, kernel_ms, sm_mhz, n_sms):
-    """Warp-instruction issue rate of the encode call against the SMs' issue
+    """Warp-instruction issue rate of the encode kernel against the SMs' issue
     peak: 4 schedulers per SM, one warp instruction each per cycle, at the SM
     clock sampled during the timed region.  The instructions per launch come
-    from the committed ncu capture of the same workload.  None without that
-    capture or without a clock sample."""
+    from the committed ncu capture of the same workload and the same CUDA
+    sources (None when the capture is of another build, or without a clock
+    sample).  kernel_ms is the CUDA-event time of the encode call: KEncode
+    plus, for the refining presets, the two block-order kernels in front of
+    it (KBlockBuckets, KBlockOrder; about 13 us of a 5.6 ms call)."""
+    prof = current_capture(prof)
     if not prof or not prof.get("warp_inst_per_launch") or not sm_mhz or not kernel_ms or kernel_ms <= 0:
         return None
     achieved = prof["warp_inst_per_launch"] / (kernel_ms / 1e3) / 1e9
     peak = 4.0 * n_sms * sm_mhz * 1e6 / 1e9
     return {"achieved": achieved, "peak": peak, "unit": "G warp-inst/s", "frac": achieved / peak,
-            "warp_inst_per_launch": prof["warp_inst_per_launch"], "source": "profiles/" + prof["summary"]}
+            "warp_inst_per_launch": prof["warp_inst_per_launch"], "source": "profiles/" + prof["summary"],
+            "capture_source_sha": prof["source_sha"]}
+
+
+def work_roofline(workload, kernel_ms, sm_mhz, n_sms):
+    """The reference's algorithmic integer work (oracle/work_counts.json:
+    int ops the reference's search performs on this workload, counted by the
+    instrumented oracle) over the encode time, against the SMs' integer-lane
+    peak (4 schedulers x 32 lanes per SM per cycle)."""
+    f = ROOT / "oracle" / "work_counts.json"
+    if not f.exists() or not sm_mhz or not kernel_ms:
+        return None
+    w = json.loads(f.read_text()).get("workloads", {}).get(workload)
+    if not w:
+        return None
+    achieved = w["int_ops"] / (kernel_ms / 1e3) / 1e12
+    peak = 128.0 * n_sms * sm_mhz * 1e6 / 1e12
+    return {"achieved": achieved, "peak": peak, "unit": "T int-op/s", "frac": achieved / peak,
+            "int_ops_per_step": w["int_ops"], "source": "oracle/work_counts.json"}
+
+
+def simd_equivalent(workload, port_value):
+    """The reference's own SIMD build on these cores, estimated: the port's
+    measured rate times the port / reference time ratio that
+    oracle/calibrate_cpu.py measured on an x86-64 host (same blocks, same
+    thread count).  None without a calibration of this workload."""
+    f = ROOT / "oracle" / "cpu_calibration.json"
+    if not f.exists() or port_value is None:
+        return None
+    cal = json.loads(f.read_text())
+    w = cal["workloads"].get(workload)
+    if not w:
+        return None
+    return {"value": port_value * w["port_time_over_reference"], "unit": "Mpx/s",
+            "port_time_over_reference": w["port_time_over_reference"],
+            "calibration": {"cpu": cal["host"]["cpu"], "threads": cal["host"]["threads"],
+                            "reference_isa": cal["host"]["reference_isa"], "sample": w["sample"],
+                            "reference_mpx_s": w["reference_mpx_s"], "port_mpx_s": w["port_mpx_s"]},
+            "kind": "estimate", "source": "oracle/cpu_calibration.json"}
 
 
 def cpu_rate(padded, mask, o, d, s, budget_s=12.0, threads=None):
@@ -279,7 +339,8 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8", "data": "synthetic",
         "config": {"workload": args.workload, "texture": f"{pw}x{ph}", "flags": WORKLOADS[args.workload][4],
                    "preset": {"denoise": d, "step": s}},
-        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "Mpx/s", "cores": threads, "kind": "port", "sample": sample,
+                         "reference_simd_equiv": simd_equivalent(args.workload, value)},
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -386,18 +447,46 @@ def run_ours(args, rank, world, local):
     algo_bytes = nblocks * (64 + (64 if mask is not None else 0) + 16 + 16)
     achieved = algo_bytes / (kernel_ms / 1e3) / 1e9
     # per-launch DRAM traffic and issue utilisation of the encode kernel, from the
-    # committed ncu capture of this workload (null when there is none)
-    traffic, issue, prof = None, None, None
+    # committed ncu capture of this workload and these CUDA sources (null otherwise)
     tf = ROOT / "profiles" / "kencode_ncu.json"
-    if tf.exists():
-        prof = json.loads(tf.read_text()).get(args.workload)
-        if prof:
-            traffic = prof["dram_bytes_per_launch"]
-            issue = {k: prof[k] for k in ("sm_issue_active_pct_elapsed", "pipe_alu_pct_active", "pipe_fma_pct_active")}
-            issue["source"] = "profiles/" + prof["summary"]
+    prof_all = json.loads(tf.read_text()) if tf.exists() else {}
+    prof = current_capture(prof_all.get(args.workload))
+    traffic, issue_ncu = None, None
+    if prof:
+        traffic = prof["dram_bytes_per_launch"]
+        issue_ncu = {k: prof[k] for k in ("sm_issue_active_pct_elapsed", "pipe_alu_pct_active", "pipe_fma_pct_active",
+                                          "warps_active_pct") if k in prof}
+        issue_ncu["source"] = "profiles/" + prof["summary"]
+    sm_mhz = None
+    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    hbm = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "traffic": traffic, "peak_source": peak_src,
+           "algorithmic_bytes_per_block": algo_bytes // nblocks}
 
     if rank == 0:
         cpu_value, cores, sample, _ = cpu_rate(padded, mask, o, d, s, budget_s=args.cpu_budget)
+        clk = clocks.summary()
+        sm_mhz = clk["sm_mhz"]
+        issue = issue_roofline(prof, kernel_ms, sm_mhz, n_sms)
+        work = work_roofline(args.workload, kernel_ms, sm_mhz, n_sms)
+        if issue:
+            roofline = {"bound": "int_issue", "achieved": issue["achieved"], "peak": issue["peak"],
+                        "unit": issue["unit"], "frac": issue["frac"], "traffic": traffic,
+                        "peak_source": "4 warp instructions per SM per cycle x SMs x sampled SM clock",
+                        "warp_inst_per_launch": issue["warp_inst_per_launch"], "source": issue["source"],
+                        "capture_source_sha": issue["capture_source_sha"]}
+        else:
+            roofline = dict(hbm)
+            roofline["issue"] = None
+        roofline.update({"kernel_ms": kernel_ms, "hbm": hbm, "issue_ncu": issue_ncu, "work": work,
+                         "build_source_sha": source_sha(),
+                         "note": "integer-issue and latency bound search. frac: executed warp instructions "
+                                 "(ncu, same CUDA sources) over the issue peak; work: the reference's algorithmic "
+                                 "int ops over the integer-lane peak; hbm: algorithmic input/output bytes, of "
+                                 "measured peak. kernel_ms covers the encode call (KBlockBuckets + KBlockOrder "
+                                 "+ KEncode for the refining presets, KEncode alone for draft)"})
+        cpu = {"value": cpu_value, "unit": "Mpx/s", "cores": cores, "kind": "port", "sample": sample,
+               "reference_simd_equiv": simd_equivalent(args.workload, cpu_value)}
         line = {
             "metric": "bc7_encode_Mpx_per_s", "value": value, "unit": "Mpx/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
@@ -408,16 +497,9 @@ def run_ours(args, rank, world, local):
             "e2e": {"value": px * world / e2e_s / 1e6, "unit": "Mpx/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps * launches_per_encode,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": traffic, "peak_source": peak_src, "kernel_ms": kernel_ms,
-                         "algorithmic_bytes_per_block": algo_bytes // nblocks, "issue_ncu": issue,
-                         "issue": issue_roofline(prof, kernel_ms, clocks.summary()["sm_mhz"],
-                                                 torch.cuda.get_device_properties(dev).multi_processor_count),
-                         "note": "integer-issue and latency bound search; HBM bytes are the algorithmic "
-                                 "input/output bytes, of measured peak; kernel_ms covers the encode call "
-                                 "(block order and KEncode)"},
-            "cpu_baseline": {"value": cpu_value, "unit": "Mpx/s", "cores": cores, "kind": "port", "sample": sample},
-            "clocks": clocks.summary(),
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk,
             "wall_s_timed": wall,
         }
         print(json.dumps(line), flush=True)

@@ -160,6 +160,7 @@ SIGNATURES = {
     "nebc7_decode_device": (I, [VP, VP, LL, I, I, VP]),
     "nebc7_decode_blocks_host": (I, [VP, VP, I]),
     "nebc7_init_device": (I, [I]),
+    "nebc7_table_read": (I, [I, I, VP, LL, ctypes.POINTER(LL)]),
     "nebc7_launch_shape": (I, [VP, VP, VP]),
     "nebc7_encode_device_noalloc": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),
     "nebc7_batch_create": (I, [VP, I, I, VP]),

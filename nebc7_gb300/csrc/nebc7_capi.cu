@@ -58,6 +58,16 @@ int SetError(int e)
 			return SetError(NEBC7_ECUDA);    \
 	} while (0)
 
+/* Bytes of each resident level table, in LevelTables order. */
+constexpr int kNumLevelTables = 14;
+constexpr size_t kLevelTableBytes[kNumLevelTables] = {
+	size_t(511) * 512, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
+	size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
+	size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
+	size_t(256) * 128 * 2, size_t(256) * 32 * 2,
+	size_t(511) * 256, size_t(511) * 256,
+};
+
 int BuildTables(int dev, int denoise, const LevelTables** out)
 {
 	std::lock_guard<std::mutex> lock(gMutex);
@@ -66,13 +76,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 	DeviceTables& D = gTables[dev][denoise];
 	if (!D.built)
 	{
-		const size_t sizes[14] = {
-			size_t(511) * 512, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
-			size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
-			size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
-			size_t(256) * 128 * 2, size_t(256) * 32 * 2,
-			size_t(511) * 256, size_t(511) * 256,
-		};
+		const size_t* sizes = kLevelTableBytes;
 		/* per-x full tables, only to build the reduced and cut tables from */
 		uint8_t* d3v8 = nullptr;
 		uint8_t* d2v8 = nullptr;
@@ -1204,6 +1208,9 @@ void FreeServer(nebc7_server* sv)
    error / SSIM sums (the layout of EncodeScratchBytes). */
 constexpr int kNoAllocMaxBlocks = 65536;
 constexpr size_t kNoAllocScratchBytes = EncodeScratchBytes(kNoAllocMaxBlocks, true);
+/* 2304 + 262144 + 65536 + 65536 * 24 + 64 bytes: about 1.9 MB on every device
+   that loads the library */
+static_assert(kNoAllocScratchBytes == 1902912, "the documented size of the allocation-free scratch");
 static __device__ __align__(256) unsigned char gNoAllocScratch[kNoAllocScratchBytes];
 
 namespace {
@@ -1487,6 +1494,23 @@ int nebc7_init_device(int denoise)
 	CK(cudaGetDevice(&dev));
 	const LevelTables* T = nullptr;
 	return BuildTables(dev, denoise, &T);
+}
+
+int nebc7_table_read(int denoise, int which, void* host, long long capacity, long long* bytes)
+{
+	if ((denoise != 0 && denoise != 1) || which < 0 || which >= kNumLevelTables || !host || !bytes)
+		return SetError(NEBC7_EINVAL);
+	int dev = 0;
+	CK(cudaGetDevice(&dev));
+	const LevelTables* T = nullptr;
+	if (int e = BuildTables(dev, denoise, &T))
+		return e;
+	const size_t n = kLevelTableBytes[which];
+	*bytes = (long long)n;
+	if (capacity < (long long)n)
+		return SetError(NEBC7_ETOOBIG);
+	CK(cudaMemcpy(host, gTables[dev][denoise].mem[which], n, cudaMemcpyDeviceToHost));
+	return NEBC7_OK;
 }
 
 int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_batch** out)

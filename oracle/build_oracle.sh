@@ -6,7 +6,7 @@
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/liboracle_port.so"
-g++ -O2 -std=c++17 -fPIC -shared -ffp-contract=off -fno-strict-aliasing \
+g++ -O3 -std=c++17 -fPIC -shared -ffp-contract=off -fno-strict-aliasing \
   "$HERE/port_tables.cpp" "$HERE/port_core.cpp" "$HERE/port_block.cpp" \
   "$HERE/port_modes.cpp" "$HERE/port_api.cpp" -o "$OUT" -lpthread
 echo "built $OUT"

@@ -5,13 +5,16 @@
 #
 #   usage: oracle/build_ref.sh [reference_src_dir]
 #
+# Without an argument the sources are taken from $NEBC7_REFERENCE_SRC, else
+# from a checkout named `reference` beside this repository.
+#
 # One shared library per (kDenoise, kDenoiseStep) preset, because the
 # reference fixes the preset at compile time (src/Bc7Mode.h:10-13).
 # -ffp-contract=off keeps the double-precision SSIM tie-break
 # (src/Bc7Core.cpp:1341-1428) unfused, as the reference's MSVC build computes it.
 set -e
-SRC=${1:-/root/reference/src}
 HERE=$(cd "$(dirname "$0")" && pwd)
+SRC=${1:-${NEBC7_REFERENCE_SRC:-$HERE/../../reference/src}}
 OUT="$HERE/_ref"
 if [ ! -d "$SRC" ]; then
   echo "reference sources not found at $SRC; skipping" >&2

@@ -85,6 +85,23 @@ def test_noalloc_matches_encode_device_twice(native, name):
     assert np.array_equal(blocks, ref_blocks)
 
 
+def test_noalloc_at_its_exact_capacity(native):
+    """A 1024x1024 texture fills the fixed scratch exactly (65536 blocks): the
+    last block's result sits at the end of the array."""
+    torch = pytest.importorskip("torch")
+    img = synth.image_for("photo_like", 1024, 1024, 15)
+    assert (1024 // 4) * (1024 // 4) == MAX_BLOCKS
+    for preset in ((1, 9, 1, 0, 0), (1, 9, 1, 1, 0)):
+        st = _settings(*preset)
+        assert native.nebc7_init_device(preset[0]) == 0
+        ref_blocks, ref_errs, ref_ssim = _encode_reference_entry(native, torch, img, None, st)
+        for _ in range(2):
+            blocks, errs, ssim = _encode_noalloc(native, torch, img, None, st)
+            assert np.array_equal(blocks, ref_blocks)
+            assert errs.tolist() == ref_errs.tolist()
+            assert np.allclose(ssim, ref_ssim, rtol=SSIM_RTOL, atol=0)
+
+
 def test_noalloc_rejects_textures_beyond_its_scratch(native):
     torch = pytest.importorskip("torch")
     dev = torch.device("cuda", 0)
