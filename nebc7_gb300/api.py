@@ -71,7 +71,8 @@ class Bc7Core:
     def init_tables(self, do_draft: bool = True, do_normal: bool = True, do_slow: bool = False,
                     linear_data: bool = False) -> None:
         """pInitTables (src/Bc7Core.cpp:1877): flags, weights and resident tables."""
-        self._flags = (bool(do_draft), bool(do_normal), bool(do_slow), bool(linear_data))
+        draft = 2 if do_draft == 2 else bool(do_draft)   # 2: the Mode6Index2 fast run
+        self._flags = (draft, bool(do_normal), bool(do_slow), bool(linear_data))
         check(self._lib.nebc7_init_device(int(self.preset.denoise)), "init tables")
 
     def weight_alpha(self) -> int:
@@ -177,6 +178,10 @@ def parse_flags(flags: str) -> dict:
             o.update(mask=False, linear=True)
         elif f == "/compare":
             o.update(draft=False, normal=False, slow=False)
+        elif f == "/m6i2":
+            # the "Mode6Index2 fast" run: the draft chain reduced to its
+            # Mode6Index2 pass (no counterpart switch in the reference CLI)
+            o.update(draft=2, normal=False, slow=False)
         elif f == "/noflip":
             pass
         else:

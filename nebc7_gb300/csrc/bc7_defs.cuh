@@ -19,6 +19,16 @@ namespace nebc7 {
 #define NEBC7_SHARED __noinline__
 #endif
 
+/* Marks the pass-level routines of the refinement and full searches (one
+   refinement, one full search of a mode, a subset search, an estimate
+   pass).  The outlined kernels define it __noinline__: with the passes
+   inlined into the kernel body its code outgrows the instruction cache, and
+   warps that sit in different passes stall on instruction fetch.  Empty
+   by default (the compiler decides). */
+#ifndef NEBC7_PASS
+#define NEBC7_PASS
+#endif
+
 /* Marks the passes a block runs once (the fast passes, the final pack).  The
    draft-only translation units define it __noinline__; in the kernels with
    the searches, out-of-line copies raise the register count (232 -> 247). */

@@ -100,7 +100,7 @@ __device__ __forceinline__ int PlaneError(const int* plane, const Area& ar, int 
 /* ---------------------------------------------------------------------- */
 
 template<int kD, int BITS>
-__device__ int AreaError(const Area& ar, int active, Ep ep, const int w[4], int water)
+__device__ NEBC7_PASS int AreaError(const Area& ar, int active, Ep ep, const int w[4], int water)
 {
 	LevelSet<BITS> Lv;
 	Lv.Init(ep);
@@ -125,7 +125,7 @@ __device__ int AreaError(const Area& ar, int active, Ep ep, const int w[4], int 
 
 /* Mode 4/5 error on Area1 (see RotErrorExact) with early exit. */
 template<int kD, int CB, int AB, bool MODE4>
-__device__ int RotErrorW(const Area& ar, const AreaInfo& ai, Ep epImg, int rotation, const int w[4], int water)
+__device__ NEBC7_PASS int RotErrorW(const Area& ar, const AreaInfo& ai, Ep epImg, int rotation, const int w[4], int water)
 {
 	const int a = RotChannel(rotation);
 	LevelSet<CB> LC;
@@ -304,7 +304,7 @@ __device__ __forceinline__ int Pbits(int mode, int v)
 
 /* Subset::InitLevels (src/Bc7CoreMode0.cpp:249-268) for variant v. */
 template<int kD, int MODE>
-__device__ bool InitLevels3(SearchState& ss, int v, const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp,
+__device__ NEBC7_PASS bool InitLevels3(SearchState& ss, int v, const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp,
 	int water, const int est[3], ChanList cl[3], int lane)
 {
 	const int pb = Pbits(MODE, v);
@@ -323,7 +323,7 @@ __device__ bool InitLevels3(SearchState& ss, int v, const Area& ar, const AreaIn
 /* Subsets (src/Bc7CoreMode0.cpp:366-415): all variants' lists start from
    the same water, then the variants are searched in order. */
 template<int kD, int MODE>
-__device__ int SearchSubset3(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
+__device__ NEBC7_PASS int SearchSubset3(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
 	int water, const int est[3], Ep& best, bool& any, int lane)
 {
 	constexpr int IB = (MODE == 0 || MODE == 1) ? 3 : 2;
@@ -344,7 +344,7 @@ __device__ int SearchSubset3(SearchState& ss, const Area& ar, const AreaInfo& ai
 }
 
 template<int kD>
-__device__ AreaInfo BuildSubset(WarpState& st, const CellRegs& R, const Params& P, Area& ar, int ns, int p, int s, int lane)
+__device__ NEBC7_PASS AreaInfo BuildSubset(WarpState& st, const CellRegs& R, const Params& P, Area& ar, int ns, int p, int s, int lane)
 {
 	const uint32_t part = ns == 3 ? c_part3[p] : c_part2[p];
 	const uint32_t member = Member(part, s);
@@ -357,7 +357,7 @@ __device__ AreaInfo BuildSubset(WarpState& st, const CellRegs& R, const Params& 
 
 /* ModeN::CompressBlock for modes 0-3 (src/Bc7CoreMode0.cpp:417-498). */
 template<int kD, int MODE>
-__device__ void RefineOpaque(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void RefineOpaque(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	constexpr int NS = (MODE == 0 || MODE == 2) ? 3 : 2;
 	constexpr int IB = (MODE == 0 || MODE == 1) ? 3 : 2;
@@ -399,7 +399,7 @@ __device__ void RefineOpaque(WarpState& st, SearchState& ss, CellRegs& R, const 
 
 /* EstimateLevels of modes 0-3 (src/Bc7CoreMode0.cpp:500-530). */
 template<int kD>
-__device__ int EstimateLevels3(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp, int water,
+__device__ NEBC7_PASS int EstimateLevels3(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const Spec3& sp, int water,
 	int est[4], int lane)
 {
 	int error = 0;
@@ -458,7 +458,7 @@ __device__ __forceinline__ void StableSortOrder(int2* order, int n, int lane)
 /* Full searches of modes 0 and 2 (src/Bc7CoreMode0.cpp:532-642,
    src/Bc7CoreMode2.cpp:456-566). */
 template<int kD, int MODE>
-__device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	constexpr int NP = MODE == 0 ? 16 : 64;
 	const Spec3 sp = GetSpec3<MODE>(T);
@@ -557,7 +557,7 @@ __device__ void FullThreeSubsets(WarpState& st, SearchState& ss, CellRegs& R, co
    src/Bc7CoreMode3.cpp:471-569); the PCA bound is zero in the reference's
    default build. */
 template<int kD, int MODE>
-__device__ void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	const Spec3 sp = GetSpec3<MODE>(T);
 	const int step = R.denoiseStep;
@@ -724,7 +724,7 @@ __device__ NEBC7_SHARED int TryVariants4(const Area& ar, const AreaInfo& ai, con
 /* Subset::InitLevels of modes 6 / 6Index2 / 7 (src/Bc7CoreMode6.cpp:1130-1161,
    src/Bc7CoreMode7.cpp:237-268). */
 template<int kD, int MODE>
-__device__ bool InitLevels4(SearchState& ss, int v, int pbits, const Area& ar, const AreaInfo& ai, const Params& P,
+__device__ NEBC7_PASS bool InitLevels4(SearchState& ss, int v, int pbits, const Area& ar, const AreaInfo& ai, const Params& P,
 	const LevelTables& T, int water, const int est[4], ChanList cl[4], int lane)
 {
 	const int wts[4] = { P.wA, P.wG, P.wR, P.wB };
@@ -772,7 +772,7 @@ __device__ int TryV4(SearchState& ss, int v, const Area& ar, const AreaInfo& ai,
 /* Mode 6 / 6Index2 CompressSubset (src/Bc7CoreMode6.cpp:1334-1364): each
    later p-bit variant starts from the water left by the earlier ones. */
 template<int kD, int MODE>
-__device__ int CompressSubsetSingle(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
+__device__ NEBC7_PASS int CompressSubsetSingle(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
 	Ep& mc, int water, int lane)
 {
 	const int est[4] = { 0, 0, 0, 0 };
@@ -788,7 +788,7 @@ __device__ int CompressSubsetSingle(SearchState& ss, const Area& ar, const AreaI
 
 /* Mode 7 Subsets (src/Bc7CoreMode7.cpp:441-494). */
 template<int kD>
-__device__ int SearchSubset7(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
+__device__ NEBC7_PASS int SearchSubset7(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T,
 	int water, const int est[4], Ep& best, bool& any, int lane)
 {
 	const int pb[4] = { 0x0101, 0, 1, 1 << 8 };
@@ -804,7 +804,7 @@ __device__ int SearchSubset7(SearchState& ss, const Area& ar, const AreaInfo& ai
 }
 
 template<int kD, int MODE>
-__device__ void RefineMode6(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void RefineMode6(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode6.cpp:1366-1381 */
 	Ep mc = R.best[0];
@@ -817,7 +817,7 @@ __device__ void RefineMode6(WarpState& st, SearchState& ss, CellRegs& R, const P
 }
 
 template<int kD>
-__device__ void FullMode6(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullMode6(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode6.cpp:1398-1422 */
 	if (R.personalMode == 6)
@@ -837,7 +837,7 @@ __device__ void FullMode6(WarpState& st, SearchState& ss, CellRegs& R, const Par
 }
 
 template<int kD>
-__device__ void RefineMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void RefineMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode7.cpp:496-557 */
 	const int p = R.bestParam;
@@ -874,7 +874,7 @@ __device__ void RefineMode7(WarpState& st, SearchState& ss, CellRegs& R, const P
 
 /* EstimateLevels of mode 7 (src/Bc7CoreMode7.cpp:574-627). */
 template<int kD>
-__device__ int EstimateLevels7(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, int water,
+__device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const AreaInfo& ai, const Params& P, const LevelTables& T, int water,
 	int est[4], int lane)
 {
 	int error = 0;
@@ -909,7 +909,7 @@ __device__ int EstimateLevels7(SearchState& ss, const Area& ar, const AreaInfo& 
 }
 
 template<int kD>
-__device__ void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode7.cpp:629-725; every partition enters with estimate step */
 	const int step = R.denoiseStep;
@@ -1062,7 +1062,7 @@ __device__ NEBC7_SHARED int TryVariantsRot(const Area& ar, const AreaInfo& ai, c
 /* Subset InitLevels of modes 4 / 5 (src/Bc7CoreMode4.cpp:1264-1322, :1505-1563,
    src/Bc7CoreMode5.cpp:628-686) + TryVariants. */
 template<int kD, int MODE>
-__device__ int CompressRotSubset(WarpState& st, SearchState& ss, const CellRegs& R, const Params& P, const LevelTables& T,
+__device__ NEBC7_PASS int CompressRotSubset(WarpState& st, SearchState& ss, const CellRegs& R, const Params& P, const LevelTables& T,
 	Ep& mcStorage, int water, int rotation, int lane)
 {
 	const Area& ar = st.area1;
@@ -1110,7 +1110,7 @@ __device__ int CompressRotSubset(WarpState& st, SearchState& ss, const CellRegs&
 }
 
 template<int kD>
-__device__ void RefineMode4(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void RefineMode4(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode4.cpp:1795-1822 */
 	int rotation = R.bestParam;
@@ -1130,7 +1130,7 @@ __device__ void RefineMode4(WarpState& st, SearchState& ss, CellRegs& R, const P
 }
 
 template<int kD>
-__device__ void RefineMode5(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void RefineMode5(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode5.cpp:890-911 */
 	Ep mc = 0;
@@ -1143,7 +1143,7 @@ __device__ void RefineMode5(WarpState& st, SearchState& ss, CellRegs& R, const P
 }
 
 template<int kD, int MODE>
-__device__ void FullRot(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullRot(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	/* src/Bc7CoreMode4.cpp:1824-1857, src/Bc7CoreMode5.cpp:913-946 */
 	const int step = R.denoiseStep;

@@ -8,6 +8,7 @@
  * bench.py as the CPU baseline.
  */
 #include "port_core.h"
+#include "port_counters.h"
 
 #include <atomic>
 #include <string.h>
@@ -87,7 +88,28 @@ void ParallelJobs(int nblocks, int threads, F&& fn, JobSums& total)
 
 } // namespace
 
+#ifdef NEBC7_PORT_COUNTERS
+namespace nebc7_oracle {
+std::atomic<uint64_t> gWork[kNumWorkCounters];
+}
+#endif
+
 extern "C" {
+
+/* The work counters (port_counters.h) since the last reset, in WorkCounter
+   order; returns how many there are (0 in the plain build). */
+int nebc7_oracle_work(uint64_t* out, int reset)
+{
+#ifdef NEBC7_PORT_COUNTERS
+	for (int i = 0; i < kNumWorkCounters; i++)
+		out[i] = reset ? gWork[i].exchange(0) : gWork[i].load();
+	return kNumWorkCounters;
+#else
+	(void)out;
+	(void)reset;
+	return 0;
+#endif
+}
 
 /* Builds the level tables for one kDenoise value ahead of timing. */
 void nebc7_oracle_init(int denoise)

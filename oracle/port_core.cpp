@@ -7,6 +7,7 @@
  * taken modulo 32, cvttps of NaN), the same behaviour is spelled out.
  */
 #include "port_core.h"
+#include "port_counters.h"
 
 #include <algorithm>
 #include <string.h>
@@ -417,7 +418,8 @@ int SubsetError(const Config& cfg, const Area& area, const uint8_t ep[8], int in
 	const int levels = 1 << indexBits;
 
 	int sum = 0;
-	for (uint32_t i = 0; i < area.active; i++)
+	uint32_t i = 0;
+	for (; i < area.active; i++)
 	{
 		int best = 0x7FFFFFFF;
 		for (int k = 0; k < levels; k++)
@@ -432,8 +434,13 @@ int SubsetError(const Config& cfg, const Area& area, const uint8_t ep[8], int in
 		}
 		sum += best;
 		if (!(water > sum))
+		{
+			i++;
 			break;
+		}
 	}
+	PORT_COUNT(kErrCalls, 1);
+	PORT_COUNT(kErrTerms, uint64_t(i) * levels * ((w[0] != 0) + (w[1] != 0) + (w[2] != 0) + (w[3] != 0)));
 	return sum;
 }
 
@@ -766,7 +773,9 @@ void ChannelLevels(const Config& cfg, Levels& L, const Area& area, int offset, i
 		top = 0xFFFF;
 	const uint32_t top16 = uint32_t(top) & 0xFFFF;
 
+	PORT_COUNT(kScanCalls, 1);
 	auto sumAt = [&](int32_t c) -> uint32_t {
+		PORT_COUNT(kScanTerms, count);
 		uint32_t s = 0;
 		for (uint32_t i = 0; i < count; i++)
 		{
@@ -940,6 +949,7 @@ void ChannelLevelsHalf(const Config& cfg, Levels& L, const Area& area, int offse
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
 	const int pL = reverse ? (pbits >> 8) : (pbits & 1);
 
+	PORT_COUNT(kScanCalls, 1);
 	for (int32_t iH = win.HL + pH; iH < win.HH; iH += 2)
 	{
 		const int32_t cH = iH << shift;
@@ -953,6 +963,7 @@ void ChannelLevelsHalf(const Config& cfg, Levels& L, const Area& area, int offse
 				if (!((flags >> (2 * j)) & 1))
 					continue;
 				const int32_t cc = c + pL + 2 * j;
+				PORT_COUNT(kScanTerms, count);
 				int32_t s = 0;
 				for (uint32_t i = 0; i < count; i++)
 				{
@@ -1023,11 +1034,13 @@ int EstimateChannelLevels(const Config& cfg, const Area& area, int offset, int w
 
 	/* rows[iH]: saturating sum of the cut (row-minimum squared) values,
 	   a lower bound for every candidate of row iH (:233-251). */
+	PORT_COUNT(kEstCalls, 1);
 	uint32_t rows[256];
 	for (int32_t iH = win.HL & ~15; iH < win.HH; iH++)
 	{
 		if (iH < 0)
 			continue;
+		PORT_COUNT(kEstTerms, count);
 		uint32_t s = 0;
 		for (uint32_t i = 0; i < count; i++)
 			s += cuts[i][iH];
@@ -1043,6 +1056,7 @@ int EstimateChannelLevels(const Config& cfg, const Area& area, int offset, int w
 		uint32_t rowBest = 0xFFFF;
 		for (int32_t iL = cH, hL = std::min(win.LH, iH) + cH; iL <= hL; iL += 32)
 		{
+			PORT_COUNT(kEstTerms, 32 * count);
 			for (int j = 0; j < 32; j++)
 			{
 				uint32_t s = 0;

@@ -10,6 +10,7 @@
  * pair errors.
  */
 #include "port_core.h"
+#include "port_counters.h"
 
 #include <string.h>
 
@@ -188,8 +189,14 @@ int RotError(const Config& cfg, const Area& area, const uint8_t epImg[8], int ro
 		sum += besta;
 		sum += bestc;
 		if (!(water > sum))
+		{
+			PORT_COUNT(kErrCalls, 1);
+			PORT_COUNT(kErrTerms, uint64_t(i + 1) * (nc * 3 + na));
 			return sum;
+		}
 	}
+	PORT_COUNT(kErrCalls, 1);
+	PORT_COUNT(kErrTerms, uint64_t(i) * (nc * 3 + na));
 	if (mode4 && i < 16)
 	{
 		int m = epImg[0] < epImg[1] ? epImg[0] : epImg[1];

@@ -6,6 +6,8 @@
 * ``Reference``: the reference encoder compiled from its own sources by
   oracle/build_ref.sh (x86 only, oracle/_ref/); used to pin ``Port`` and to
   generate the committed golden fixtures.
+* ``ReferenceCli``: the reference's command-line build (its own
+  configuration, the real job pool, the /map and /bad outputs).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU baseline use this.
 """
@@ -83,10 +85,12 @@ class Port:
 
 
 class Reference:
-    """The reference encoder built from its sources (one library per preset)."""
+    """The reference encoder built from its sources (one library per preset).
+    variant "m6i2": its draft chain reduced to the Mode6Index2 pass
+    (oracle/ref_m6i2_only.cpp; default preset only)."""
 
-    def __init__(self, denoise: int, step: int):
-        path = REF_DIR / f"libnebc7_ref_d{denoise}s{step}.so"
+    def __init__(self, denoise: int, step: int, variant: str = ""):
+        path = REF_DIR / f"libnebc7_ref_d{denoise}s{step}{'_' + variant if variant else ''}.so"
         if not path.exists():
             raise FileNotFoundError(f"{path} (run oracle/build_ref.sh on an x86-64 host with the reference sources)")
         L = ctypes.CDLL(str(path))
@@ -116,3 +120,28 @@ class Reference:
                                              _p(err), _p(ssim))
         assert rc == 0, rc
         return out.reshape(-1, 16), err, ssim
+
+
+class ReferenceCli:
+    """The reference's command-line build (oracle/ref_cli_shim.h): runs its
+    CLI driver on an in-memory image and returns the encoded blocks and the
+    /map and /bad images (padded BGRA, top-down)."""
+
+    def __init__(self):
+        path = REF_DIR / "libnebc7_ref_cli.so"
+        if not path.exists():
+            raise FileNotFoundError(f"{path} (run oracle/build_ref.sh on an x86-64 host with the reference sources)")
+        L = ctypes.CDLL(str(path))
+        L.nebc7_ref_cli.argtypes = [VP, I, I, ctypes.c_char_p, VP, I, VP, VP]
+        self.lib = L
+
+    def run(self, img, flags):
+        h, w = img.shape[:2]
+        pw, ph = (max(4, w) + 3) & ~3, (max(4, h) + 3) & ~3
+        blocks = np.zeros(pw * ph, np.uint8)
+        mp = np.zeros((ph, pw, 4), np.uint8)
+        bad = np.zeros((ph, pw, 4), np.uint8)
+        img = np.ascontiguousarray(img)
+        rc = self.lib.nebc7_ref_cli(_p(img), w, h, flags.encode(), _p(blocks), blocks.size, _p(mp), _p(bad))
+        assert rc == 7, rc
+        return blocks.reshape(-1, 16), mp, bad

@@ -49,7 +49,7 @@ def needs(native, st):
 
 
 SETS = ["d1s9_draft", "d1s9_draft_restart", "d0s0_draft", "d1s9_normal", "d1s9_slow", "d1s9_normal_restart",
-        "d0s0_normal", "d0s0_slow", "d1s0_normal", "d0s9_normal", "d1s9_linear"]
+        "d0s0_normal", "d0s0_slow", "d1s0_normal", "d0s9_normal", "d1s9_linear", "d1s9_m6i2", "d1s9_m6i2_restart"]
 
 
 @pytest.mark.parametrize("name", SETS)
@@ -90,7 +90,7 @@ def test_blocks_match_oracle(native, port, seed, preset, passes):
 
 IMAGES = ["cfg1_256_draft", "cfg1_256_default", "cfg2_1024_draft", "cfg2_1024_default", "cfg2_1024_precise",
           "odd_130x98_default", "alpha_256_mask", "alpha_256_retina_precise", "tiny_3x5_default",
-          "cfg3_2048_slow", "cfg3_2048_data"]
+          "cfg3_2048_slow", "cfg3_2048_data", "cfg2_1024_m6i2", "alpha_256_m6i2"]
 
 
 @pytest.mark.parametrize("name", IMAGES)

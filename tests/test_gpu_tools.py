@@ -81,3 +81,37 @@ def test_partition_map_matches_oracle(native, port):
     out = np.zeros((len(got), 64), np.uint8)
     assert native.nebc7_decode_blocks_host(np.ascontiguousarray(got).ctypes.data, out.ctypes.data, len(got)) == 0
     assert np.array_equal(out, port.decompress_blocks(got))
+
+
+REF_CLI = ["tools_alpha_96x64_draft", "tools_alpha_96x64_data", "tools_photo_64_default", "tools_alpha_62x46_slow"]
+
+
+@pytest.mark.parametrize("name", REF_CLI)
+def test_device_bad_and_map_match_reference_cli(native, port, golden, name):
+    """The device /bad and /map steps on the reference CLI's own blocks give
+    the images the reference CLI wrote (tests/golden/tools_*.npz)."""
+    torch = pytest.importorskip("torch")
+    from nebc7_gb300.api import parse_flags
+    from conftest import GOLDEN
+    g = golden["tools"][name]
+    f = np.load(GOLDEN / f"{name}.npz")
+    o = parse_flags(g["flags"])
+    img = synth.image_for(g["kind"], g["w"], g["h"], g["seed"])
+    padded, mask = port.prepare(img, o["radius"] if o["mask"] else -1)
+    ph, pw = padded.shape[:2]
+    d_img = _dev(torch, padded)
+    d_mask = _dev(torch, mask) if o["mask"] else None
+    d_blocks = _dev(torch, f["blocks"])
+    d_dec = torch.zeros_like(d_img)
+    assert native.nebc7_decode_device(d_blocks.data_ptr(), d_dec.data_ptr(), pw * 4, pw, ph, None) == 0
+    d_bad = torch.zeros_like(d_img)
+    assert native.nebc7_bad_blocks_device(d_img.data_ptr(), d_dec.data_ptr(),
+                                          d_mask.data_ptr() if d_mask is not None else None, pw * 4, pw, ph,
+                                          int(o["linear"]), d_bad.data_ptr(), None) == 0
+    d_vis = torch.zeros_like(d_blocks)
+    assert native.nebc7_partition_map_device(d_blocks.data_ptr(), d_vis.data_ptr(), len(f["blocks"]), None) == 0
+    d_map = torch.zeros_like(d_img)
+    assert native.nebc7_decode_device(d_vis.data_ptr(), d_map.data_ptr(), pw * 4, pw, ph, None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(d_bad.cpu().numpy().reshape(ph, pw, 4), f["bad"])
+    assert np.array_equal(d_map.cpu().numpy().reshape(ph, pw, 4), f["map"])

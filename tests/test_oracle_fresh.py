@@ -24,15 +24,19 @@ PRESETS = {
     "d0s0_slow": (0, 0, 1, 1, 1, 0, 96),
     "d1s0_normal": (1, 0, 1, 1, 0, 0, 256),
     "d0s9_normal": (0, 9, 1, 1, 0, 0, 256),
+    "d1s9_m6i2": (1, 9, 2, 0, 0, 0, 1024),
 }
 SEEDS = [9001]
 
 
-def _reference(denoise, step):
+def _reference(denoise, step, draft=1):
+    """The reference build of a preset; draft 2 (the Mode6Index2 fast run)
+    is its m6i2 variant run with doDraft set."""
     from oracle.pyoracle import REF_DIR, Reference
-    if not (REF_DIR / f"libnebc7_ref_d{denoise}s{step}.so").exists():
+    variant = "m6i2" if draft == 2 else ""
+    if not (REF_DIR / f"libnebc7_ref_d{denoise}s{step}{'_' + variant if variant else ''}.so").exists():
         pytest.skip("reference build not present (x86 host with the reference sources only)")
-    return Reference(denoise, step)
+    return Reference(denoise, step, variant)
 
 
 @pytest.mark.parametrize("seed", SEEDS)
@@ -40,11 +44,11 @@ def _reference(denoise, step):
 @pytest.mark.parametrize("name", sorted(PRESETS))
 def test_port_matches_reference_on_fresh_blocks(port, name, start, seed):
     d, s, draft, normal, slow, linear, n = PRESETS[name]
-    ref = _reference(d, s)
+    ref = _reference(d, s, draft)
     cells, masks = synth.random_blocks(n, seed)
     starts = synth.random_start_blocks(n, seed + 1) if start == "random" else np.zeros((n, 16), np.uint8)
     io_ref = starts.copy()
-    err_ref, ssim_ref = ref.compress_blocks(cells, masks, io_ref, draft, normal, slow, linear, threads=8)
+    err_ref, ssim_ref = ref.compress_blocks(cells, masks, io_ref, min(draft, 1), normal, slow, linear, threads=8)
     io_port = starts.copy()
     err_port, ssim_port = port.compress_blocks(cells, masks, io_port, d, s, draft, normal, slow, linear, threads=8)
     differ = int(np.count_nonzero((io_port != io_ref).any(1)))
@@ -61,6 +65,7 @@ IMAGES = [
     ("gradient_noise", 37, 29, 34, "/noflip /draft", 1, 9),
     ("gradient_noise", 16, 12, 35, "/nomask /noflip /data", 1, 9),
     ("alpha_blobs", 28, 20, 36, "/noflip /retina", 0, 0),
+    ("alpha_blobs", 64, 40, 37, "/noflip /m6i2", 1, 9),
 ]
 
 
@@ -68,9 +73,10 @@ IMAGES = [
 def test_port_matches_reference_on_fresh_images(port, case):
     from nebc7_gb300.api import parse_flags
     kind, w, h, seed, flags, d, s = case
-    ref = _reference(d, s)
+    o = parse_flags(flags)
+    ref = _reference(d, s, o["draft"])
     img = synth.image_for(kind, w, h, seed)
-    out_ref, err_ref, ssim_ref = ref.encode_image(img, flags)
+    out_ref, err_ref, ssim_ref = ref.encode_image(img, flags.replace("/m6i2", "/draft"))
     o = parse_flags(flags)
     padded, mask = port.prepare(img, o["radius"] if o["mask"] else -1)
     out = np.zeros((padded.shape[0] // 4 * (padded.shape[1] // 4), 16), np.uint8)

@@ -32,7 +32,8 @@ def test_synthetic_inputs_reproduce(golden, blocks_input):
 
 
 SETS = ["d1s9_draft", "d1s9_normal", "d1s9_slow", "d1s9_normal_restart", "d1s9_draft_restart",
-        "d0s0_draft", "d0s0_normal", "d0s0_slow", "d1s0_normal", "d0s9_normal", "d1s9_linear"]
+        "d0s0_draft", "d0s0_normal", "d0s0_slow", "d1s0_normal", "d0s9_normal", "d1s9_linear",
+        "d1s9_m6i2", "d1s9_m6i2_restart"]
 
 
 @pytest.mark.parametrize("name", SETS)
@@ -49,7 +50,8 @@ def test_port_blocks_match_reference(port, golden, blocks_input, name):
 
 
 @pytest.mark.parametrize("name", ["cfg1_256_default", "cfg1_256_draft", "cfg2_1024_draft", "cfg2_1024_default",
-                                  "odd_130x98_default", "alpha_256_mask", "tiny_3x5_default"])
+                                  "odd_130x98_default", "alpha_256_mask", "tiny_3x5_default", "cfg2_1024_m6i2",
+                                  "alpha_256_m6i2"])
 def test_port_images_match_reference(port, golden, name):
     from nebc7_gb300.api import parse_flags
     g = golden["images"][name]
@@ -94,9 +96,10 @@ def test_port_tables_match_reference():
 
 
 def test_port_mode6index2_only_run(port, blocks_input):
-    """The "Mode6Index2 fast" run (doDraft 2, no counterpart in the reference):
-    every block stays the starting block or becomes a mode 6 block, and the
-    error is never below the full draft chain's."""
+    """The "Mode6Index2 fast" run (doDraft 2; the reference's m6i2 variant,
+    oracle/ref_m6i2_only.cpp, pins it above): every block stays the starting
+    block or becomes a mode 6 block, and the error is never below the full
+    draft chain's."""
     cells, masks, _ = blocks_input
     io6 = np.zeros((len(cells), 16), np.uint8)
     e6, _ = port.compress_blocks(cells, masks, io6, 1, 9, 2, 0, 0, 0, threads=4)
