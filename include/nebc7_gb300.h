@@ -249,6 +249,13 @@ typedef struct nebc7_request_info
 	double latency_ms;   /* submit -> its blocks were back in host memory */
 	int64_t errs[2];     /* as nebc7_encode_host reports them */
 	double ssim[2];
+	/* when it was submitted, launched and back in host memory (ms since the
+	   server's creation), the launch slot and the launch's sequence number:
+	   requests of different launches whose [launch_at, done_at] spans
+	   overlap ran on the device at the same time */
+	double submit_at_ms, launch_at_ms, done_at_ms;
+	int slot;
+	long long launch;
 } nebc7_request_info;
 
 typedef struct nebc7_server_counters

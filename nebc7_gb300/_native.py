@@ -125,7 +125,8 @@ class ServerConfig(ctypes.Structure):
 
 class RequestInfo(ctypes.Structure):
     _fields_ = [("status", I), ("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
-                ("errs", ctypes.c_int64 * 2), ("ssim", ctypes.c_double * 2)]
+                ("errs", ctypes.c_int64 * 2), ("ssim", ctypes.c_double * 2), ("submit_at_ms", ctypes.c_double),
+                ("launch_at_ms", ctypes.c_double), ("done_at_ms", ctypes.c_double), ("slot", I), ("launch", LL)]
 
 
 class ServerCounters(ctypes.Structure):

@@ -378,7 +378,9 @@ class Server:
         check(rc, "server_wait")
         self._keep.pop(ticket, None)
         return {"queue_ms": info.queue_ms, "latency_ms": info.latency_ms, "errs": [info.errs[0], info.errs[1]],
-                "ssim": [info.ssim[0], info.ssim[1]]}
+                "ssim": [info.ssim[0], info.ssim[1]], "submit_at_ms": info.submit_at_ms,
+                "launch_at_ms": info.launch_at_ms, "done_at_ms": info.done_at_ms, "slot": info.slot,
+                "launch": info.launch}
 
     def stats(self) -> dict:
         c = _native.ServerCounters()

@@ -73,6 +73,106 @@ struct BlockRef
 	BlockResult* result;     /* optional */
 };
 
+/* The draft chain (src/Bc7Core.cpp:1537-1597) after the block's stepping
+   values are set: the fast passes of modes 6Index2, 6, 4, 5, 7 with error
+   stepping, then, for blocks whose alpha stays above 239, the fast passes of
+   the opaque modes 3, 1, 2, 0. */
+template<int kD>
+__device__ __forceinline__ void DraftChain(WarpState& st, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+{
+	const int step = R.denoiseStep;
+	if (P.doDraft == 2)
+	{
+		/* the "Mode6Index2 fast" run: the draft chain reduced to its
+		   first pass (no counterpart in the reference) */
+		if (R.errTotal > step && (kD > 0 || P.denoiseStep > 0))
+			FastMode6<kD, true>(st, R, P, T);
+	}
+	else if (R.errTotal > step)
+	{
+		if (kD > 0 || P.denoiseStep > 0)
+			FastMode6<kD, true>(st, R, P, T);
+		if (R.errTotal > step)
+		{
+			FastMode6<kD, false>(st, R, P, T);
+			if (R.errTotal > step)
+			{
+				FastRot<kD, 4>(st, R, P, lane);
+				if (R.errTotal > step)
+				{
+					FastRot<kD, 5>(st, R, P, lane);
+					if (R.errTotal > step)
+						FastMode7<kD>(st, R, P, T, lane);
+				}
+			}
+		}
+	}
+
+	if (P.doDraft != 2 && int(int16_t(R.a1.minmax[0])) > 255 - 16)
+	{
+		const int gate = R.opaqueAlphaError + step;
+		if (R.errTotal > gate)
+		{
+			FastOpaque<kD, 3>(st, R, P, lane);
+			if (R.errTotal > gate)
+			{
+				FastOpaque<kD, 1>(st, R, P, lane);
+				if (R.errTotal > gate)
+				{
+					FastOpaque<kD, 2>(st, R, P, lane);
+					if (R.errTotal > gate)
+						FastOpaque<kD, 0>(st, R, P, lane);
+				}
+			}
+		}
+	}
+}
+
+/* Coalesced load of one block (lanes 0..15 a BGRA pixel each, 16..31 its
+   mask), the masked data (src/Bc7Core.cpp:52-86) and the block-wide
+   visibility and opacity. */
+__device__ __forceinline__ void LoadCell(WarpState& st, const BlockRef& b, CellRegs& R, int lane)
+{
+	{
+		const int i = lane & 15;
+		const long long off = (long long)(i >> 2) * b.stride + (i & 3) * 4;
+		if (lane < 16)
+		{
+			const uchar4 p = *reinterpret_cast<const uchar4*>(b.bgra + off);
+			st.img[i][0] = p.w;
+			st.img[i][1] = p.y;
+			st.img[i][2] = p.z;
+			st.img[i][3] = p.x;
+		}
+		else
+		{
+			uchar4 m = make_uchar4(0xFF, 0xFF, 0xFF, 0xFF);
+			if (b.mask)
+				m = *reinterpret_cast<const uchar4*>(b.mask + off);
+			st.msk[i][0] = m.x;
+			st.msk[i][1] = m.y;
+			st.msk[i][2] = m.z;
+			st.msk[i][3] = m.w;
+		}
+	}
+	__syncwarp();
+	uint32_t visBit = 0;
+	unsigned alphaAnd = 0xFF;
+	if (lane < 16)
+	{
+		for (int c = 0; c < 4; c++)
+		{
+			const uint16_t m = uint16_t(int16_t(int8_t(st.msk[lane][c])));
+			st.mk[lane][c] = m;
+			st.px[lane][c] = uint16_t(st.img[lane][c] & m);
+		}
+		visBit = (st.mk[lane][1] >> lane) & 1;
+		alphaAnd = st.px[lane][0];
+	}
+	R.visible = __ballot_sync(kFull, visBit != 0) & 0xFFFF;
+	R.opaque = __reduce_and_sync(kFull, alphaAnd) == 255;
+}
+
 template<int kD, bool NORMAL>
 __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b, const LevelTables& T, const Params& P, int lane)
 {
@@ -160,51 +260,7 @@ __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b,
 			}
 			const int water = R.errTotal;
 
-			if (P.doDraft == 2)
-			{
-				/* the "Mode6Index2 fast" run: the draft chain reduced to its
-				   first pass (no counterpart in the reference) */
-				if (R.errTotal > step && (kD > 0 || P.denoiseStep > 0))
-					FastMode6<kD, true>(st, R, P, T);
-			}
-			else if (R.errTotal > step)
-			{
-				if (kD > 0 || P.denoiseStep > 0)
-					FastMode6<kD, true>(st, R, P, T);
-				if (R.errTotal > step)
-				{
-					FastMode6<kD, false>(st, R, P, T);
-					if (R.errTotal > step)
-					{
-						FastRot<kD, 4>(st, R, P, lane);
-						if (R.errTotal > step)
-						{
-							FastRot<kD, 5>(st, R, P, lane);
-							if (R.errTotal > step)
-								FastMode7<kD>(st, R, P, T, lane);
-						}
-					}
-				}
-			}
-
-			if (P.doDraft != 2 && int(int16_t(R.a1.minmax[0])) > 255 - 16)
-			{
-				const int gate = R.opaqueAlphaError + step;
-				if (R.errTotal > gate)
-				{
-					FastOpaque<kD, 3>(st, R, P, lane);
-					if (R.errTotal > gate)
-					{
-						FastOpaque<kD, 1>(st, R, P, lane);
-						if (R.errTotal > gate)
-						{
-							FastOpaque<kD, 2>(st, R, P, lane);
-							if (R.errTotal > gate)
-								FastOpaque<kD, 0>(st, R, P, lane);
-						}
-					}
-				}
-			}
+			DraftChain<kD>(st, R, P, T, lane);
 
 			if (NORMAL && P.doNormal && P.doDraft != 2)
 				NormalPasses<kD>(st, *ss, R, P, T, lane);
@@ -244,10 +300,8 @@ __device__ void EncodeBlockAt(WarpState& st, SearchState* ss, const BlockRef& b,
 	__syncwarp();
 }
 
-/* Encodes queue position k of the launch. */
-template<int kD, bool NORMAL>
-__device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T0,
-	const LevelTables& T1, int k, int lane)
+/* Texture and block of queue position k of the launch. */
+__device__ __forceinline__ void QueuedBlock(const Job& job, int k, TexDesc& d, BlockRef& b)
 {
 	if (job.order)
 		k = job.order[k];
@@ -266,7 +320,6 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 	}
 	/* a copy, read from the table or from the launch's parameters (no
 	   pointer into the parameters, which would put them in local memory) */
-	TexDesc d;
 	if (job.tex)
 		d = job.tex[t];
 	else
@@ -274,12 +327,38 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 	const int local = k - d.first;
 	const int bx = local % d.blocksW, by = local / d.blocksW;
 	const long long base = (long long)by * 4 * d.stride + (long long)bx * 16;
-	BlockRef b;
 	b.bgra = d.bgra + base;
 	b.mask = d.mask ? d.mask + base : nullptr;
 	b.stride = d.stride;
 	b.out = d.dst + (long long)local * 16;
 	b.result = d.results ? d.results + local : (job.results ? job.results + k : nullptr);
+}
+
+/* Publishes a finished block of a request-loop texture: counts it and lets
+   the last one tell the host that the texture is complete. */
+__device__ __forceinline__ void BlockFinished(const TexDesc& d, int lane)
+{
+	if (d.remaining && lane == 0)
+	{
+		/* lane 0 wrote the block and its result: publish them first */
+		__threadfence();
+		if (atomicSub(d.remaining, 1) == 1)
+		{
+			__threadfence_system();
+			*reinterpret_cast<volatile int*>(d.doneFlag) = 1;
+		}
+	}
+	__syncwarp();
+}
+
+/* Encodes queue position k of the launch. */
+template<int kD, bool NORMAL>
+__device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, const Job& job, const LevelTables& T0,
+	const LevelTables& T1, int k, int lane)
+{
+	TexDesc d;
+	BlockRef b;
+	QueuedBlock(job, k, d, b);
 	const Params P = d.P;
 	if (kD == kAnyDenoise)
 	{
@@ -290,18 +369,7 @@ __device__ __forceinline__ void EncodeQueued(WarpState& st, SearchState* ss, con
 	}
 	else
 		EncodeBlockAt<kD == 1 ? 1 : 0, NORMAL>(st, ss, b, kD ? T1 : T0, P, lane);
-	if (d.remaining && lane == 0)
-	{
-		/* lane 0 wrote the block and its result: publish them, count the block
-		   and let the last one tell the host that the texture is complete */
-		__threadfence();
-		if (atomicSub(d.remaining, 1) == 1)
-		{
-			__threadfence_system();
-			*reinterpret_cast<volatile int*>(d.doneFlag) = 1;
-		}
-	}
-	__syncwarp();
+	BlockFinished(d, lane);
 }
 
 /* Dynamic shared memory of one encode CTA: the per-warp block state and,

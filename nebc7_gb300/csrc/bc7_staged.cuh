@@ -1,0 +1,454 @@
+/*
+ * BC7 block encoder for sm_103a -- the staged encode of the presets whose
+ * time goes to the full searches (precise, /slow, /data, mixed batches).
+ *
+ * The per-block pipeline of src/Bc7Core.cpp:1516-1823 runs as a sequence of
+ * persistent kernels instead of one: the draft chain, then one kernel per
+ * refinement / full-search pass of the normal and slow chains
+ * (src/Bc7Core.cpp:1604-1745), then the final pack, self-check and quality
+ * sums.  Every kernel holds the code of one pass only, so the warps of an SM
+ * run the same few kilobytes of instructions; in a single kernel whose warps
+ * sit in different passes the instruction working set outgrows the
+ * instruction cache and most issue slots are lost to instruction fetch.
+ *
+ * Between kernels a block's state (the reference's Cell scalars: best
+ * endpoints, mode, partition, errors, stepping values, the starting block)
+ * is kept in a BlockRecord per queue position; the pixel data and the
+ * whole-block area are rebuilt from the texture when a pass starts.  Each
+ * pass kernel runs the blocks whose next pass it is, in queue order (widest
+ * pixel range first), gathered by KStageList.  The passes, their order and
+ * their entry conditions are those of NormalPasses, so the blocks are the
+ * same bits as the single-kernel encode's.
+ */
+#pragma once
+
+#include "bc7_encode.cuh"
+
+namespace nebc7 {
+
+/* The passes after the draft chain, in chain order; kStepFinish packs. */
+enum StageStep
+{
+	kStepRefine = 0,
+	kStepFull3Mode2,
+	kStepFull3Mode0,
+	kStepFull2Mode1,
+	kStepFull2Mode3,
+	kStepRot5,
+	kStepRot4,
+	kStepMode7,
+	kStepMode6,
+	kStepFinish,
+	kNumStages
+};
+
+constexpr int kStageDraft = -1;
+constexpr int kStepNone = -1;   /* finished in the draft kernel */
+
+/* A block's Cell scalars between pass kernels. */
+struct __align__(16) BlockRecord
+{
+	Ep best[3];
+	uint64_t startLo, startHi;   /* the starting block (self-check fallback) */
+	int bestParam, bestMode, opaqueAlphaError, errAlpha;
+	int errTotal, personalParam, personalMode, denoiseStep;
+	int water;                   /* the error at the start of the draft chain */
+	int pad[3];
+};
+
+/* Per-launch state of a staged encode (one entry per queue position). */
+struct Stages
+{
+	BlockRecord* rec;
+	int* next;        /* the pass a position waits for, kStepFinish, or kStepNone */
+	int* list;        /* positions of the pass being run, in queue order */
+	int* count;       /* [kNumStages] list lengths */
+	int* counters;    /* [kNumStages + 1] work-queue heads, zero before the draft kernel */
+};
+
+__device__ __forceinline__ void SaveRecord(BlockRecord& r, const CellRegs& R, int lane)
+{
+	if (lane == 0)
+	{
+		r.best[0] = R.best[0];
+		r.best[1] = R.best[1];
+		r.best[2] = R.best[2];
+		r.bestParam = R.bestParam;
+		r.bestMode = R.bestMode;
+		r.opaqueAlphaError = R.opaqueAlphaError;
+		r.errAlpha = R.errAlpha;
+		r.errTotal = R.errTotal;
+		r.personalParam = R.personalParam;
+		r.personalMode = R.personalMode;
+		r.denoiseStep = R.denoiseStep;
+	}
+}
+
+/* Rebuilds a block's state: its pixels and masks, the saved scalars, the
+   whole-block area (src/Bc7Core.cpp:1532-1535). */
+__device__ __forceinline__ void RestoreBlock(WarpState& st, CellRegs& R, const BlockRef& b, const BlockRecord& r, const Params& P,
+	int lane)
+{
+	LoadCell(st, b, R, lane);
+	R.best[0] = r.best[0];
+	R.best[1] = r.best[1];
+	R.best[2] = r.best[2];
+	R.bestParam = r.bestParam;
+	R.bestMode = r.bestMode;
+	R.opaqueAlphaError = r.opaqueAlphaError;
+	R.errAlpha = r.errAlpha;
+	R.errTotal = r.errTotal;
+	R.personalParam = r.personalParam;
+	R.personalMode = r.personalMode;
+	R.denoiseStep = r.denoiseStep;
+	R.a1 = AreaStats(st, R, P, 0xFFFF);
+	R.a1.zero = 0;
+	BuildAreaList(st.area1, st, R, 0xFFFF, 0, lane);
+}
+
+/* One pass of the normal / slow chains (the bodies of NormalPasses). */
+template<int kD, int S>
+__device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+{
+	if constexpr (S == kStepRefine)
+	{
+		const int OA = R.opaqueAlphaError;
+		switch (R.bestMode)
+		{
+		case 0: if (R.errTotal > OA) RefineOpaque<kD, 0>(st, ss, R, P, T, lane); break;
+		case 1: if (R.errTotal > OA) RefineOpaque<kD, 1>(st, ss, R, P, T, lane); break;
+		case 2: if (R.errTotal > OA) RefineOpaque<kD, 2>(st, ss, R, P, T, lane); break;
+		case 3: if (R.errTotal > OA) RefineOpaque<kD, 3>(st, ss, R, P, T, lane); break;
+		case 4: if (R.errTotal > 0) RefineMode4<kD>(st, ss, R, P, T, lane); break;
+		case 5: if (R.errTotal > 0) RefineMode5<kD>(st, ss, R, P, T, lane); break;
+		case 6: if (R.errTotal > 0) RefineMode6<kD, 6>(st, ss, R, P, T, lane); break;
+		case 7: if (R.errTotal > 0) RefineMode7<kD>(st, ss, R, P, T, lane); break;
+		case 9: if (R.errTotal > 0) RefineMode6<kD, 9>(st, ss, R, P, T, lane); break;
+		}
+		R.personalParam = R.bestParam;
+		R.personalMode = R.bestMode;
+	}
+	else if constexpr (S == kStepFull3Mode2)
+		FullThreeSubsets<kD, 2>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepFull3Mode0)
+		FullThreeSubsets<kD, 0>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepFull2Mode1)
+		FullTwoSubsets<kD, 1>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepFull2Mode3)
+		FullTwoSubsets<kD, 3>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepRot5)
+		FullRot<kD, 5>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepRot4)
+		FullRot<kD, 4>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepMode7)
+		FullMode7<kD>(st, ss, R, P, T, lane);
+	else if constexpr (S == kStepMode6)
+		FullMode6<kD>(st, ss, R, P, T, lane);
+}
+
+/* The pass after S: the nesting of the normal and slow chains in
+   NormalPasses (src/Bc7Core.cpp:1677-1745), whose conditions are tested
+   when each pass is reached. */
+__device__ __forceinline__ int NextStep(int S, const CellRegs& R, const Params& P)
+{
+	const int OA = R.opaqueAlphaError, step = R.denoiseStep, e = R.errTotal;
+	if (R.a1.opaque)
+	{
+		switch (S)
+		{
+		case kStepRefine: return e > OA + step ? kStepFull3Mode2 : kStepFinish;
+		case kStepFull3Mode2: return e > OA + step ? kStepFull3Mode0 : kStepFinish;
+		case kStepFull3Mode0: return (P.doSlow && e > OA + step) ? kStepFull2Mode1 : kStepFinish;
+		case kStepFull2Mode1: return e > OA + step ? kStepFull2Mode3 : kStepFinish;
+		case kStepFull2Mode3: return e > step ? kStepRot5 : kStepFinish;
+		case kStepRot5: return e > step ? kStepRot4 : kStepFinish;
+		case kStepRot4: return e > step ? kStepMode7 : kStepFinish;
+		case kStepMode7: return e > step ? kStepMode6 : kStepFinish;
+		default: return kStepFinish;
+		}
+	}
+	switch (S)
+	{
+	case kStepRefine: return e > step ? kStepRot5 : kStepFinish;
+	case kStepRot5: return e > step ? kStepRot4 : kStepFinish;
+	case kStepRot4: return e > step ? kStepMode7 : kStepFinish;
+	case kStepMode7: return (P.doSlow && e > step) ? kStepMode6 : kStepFinish;
+	default: return kStepFinish;
+	}
+}
+
+/* Writes the block and its result (src/Bc7Core.cpp:1976-1984). */
+template<int kD>
+__device__ __forceinline__ void StoreBlock(const BlockRef& b, const CellRegs& R, uint64_t lo, uint64_t hi, double qa, double qc,
+	int lane)
+{
+	if (lane == 0)
+	{
+		*reinterpret_cast<uint4*>(b.out) = make_uint4(unsigned(lo), unsigned(lo >> 32), unsigned(hi), unsigned(hi >> 32));
+		if (b.result)
+		{
+			BlockResult r;
+			r.errAlpha = int(unsigned(R.errAlpha) << (kD + kD));
+			r.errColor = int(unsigned(R.errTotal - R.errAlpha) << (kD + kD));
+			r.ssimAlpha = qa;
+			r.ssimColor = qc;
+			*b.result = r;
+		}
+	}
+	__syncwarp();
+}
+
+/* The final pack when the search beat the starting block, then the
+   self-check (src/Bc7Core.cpp:1799-1807) and the SSIM sums. */
+template<int kD>
+__device__ __forceinline__ void FinishBlock(WarpState& st, CellRegs& R, const Params& P, int water, uint64_t startLo, uint64_t startHi,
+	const BlockRef& b, int lane)
+{
+	uint64_t lo = startLo, hi = startHi;
+	if (water > R.errTotal)
+		FinalPack<kD>(st, R, P, lo, hi, lane);
+	Ep dummy[3];
+	int dp, dm;
+	DecodeToState(st, lo, hi, dummy, dp, dm, lane);
+	int ea, et;
+	CompareBlocks<kD>(st, P, lane, ea, et);
+	if (ea != R.errAlpha || et != R.errTotal)
+	{
+		lo = startLo;
+		hi = startHi;
+	}
+	double qa = 1.0, qc = 1.0;
+	CompareBlocksSSIM(st, P, lane, qa, qc);
+	StoreBlock<kD>(b, R, lo, hi, qa, qc, lane);
+}
+
+/* The draft kernel's block: EncodeBlockAt up to the normal passes.  A block
+   that goes on to them saves its record and waits; the others finish here.
+   Returns whether the block finished. */
+template<int kD>
+__device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& T, const Params& P, BlockRecord& rec, int& next,
+	int lane)
+{
+	CellRegs R;
+	LoadCell(st, b, R, lane);
+	const uint4 blk = *reinterpret_cast<const uint4*>(b.out);
+	uint64_t lo = uint64_t(blk.x) | (uint64_t(blk.y) << 32);
+	uint64_t hi = uint64_t(blk.z) | (uint64_t(blk.w) << 32);
+	if (!(lo & 0xFF))
+	{
+		/* src/Bc7Core.cpp:1518-1522: an empty block starts as a zero mode 6 block */
+		lo = 1u << 6;
+		hi = 0;
+	}
+	DecodeToState(st, lo, hi, R.best, R.bestParam, R.bestMode, lane);
+	CompareBlocks<kD>(st, P, lane, R.errAlpha, R.errTotal);
+	if (!(R.errTotal > 0))
+	{
+		StoreBlock<kD>(b, R, lo, hi, 1.0, 1.0, lane);
+		if (lane == 0)
+			next = kStepNone;
+		return true;
+	}
+	R.a1 = AreaStats(st, R, P, 0xFFFF);
+	R.a1.zero = 0;
+	BuildAreaList(st.area1, st, R, 0xFFFF, 0, lane);
+	R.personalMode = -1;
+	R.personalParam = -1;
+	int water = R.errTotal;
+	if (P.doDraft)
+	{
+		const int step = R.a1.active * ((P.denoiseStep * (R.a1.opaque ? P.wColor : P.wColorAlpha)) >> (kD + kD));
+		R.denoiseStep = step;
+		/* src/Bc7Core.cpp:24-50 */
+		{
+			int e = 0;
+			if (!R.a1.opaque && lane < 16)
+			{
+				int da = int(st.area1.px[lane][0]) ^ 255;
+				da = kD ? (da >> kD) : (da > 0x7F ? 0x7F : da);
+				e = da * da;
+			}
+			e = int(__reduce_add_sync(kFull, unsigned(e)));
+			R.opaqueAlphaError = R.a1.opaque ? 0 : e * P.wA;
+		}
+		water = R.errTotal;
+		DraftChain<kD>(st, R, P, T, lane);
+		if (P.doNormal && P.doDraft != 2)
+		{
+			SaveRecord(rec, R, lane);
+			if (lane == 0)
+			{
+				rec.startLo = lo;
+				rec.startHi = hi;
+				rec.water = water;
+				next = kStepRefine;
+			}
+			__syncwarp();
+			return false;
+		}
+	}
+	else
+	{
+		/* no draft chain: the starting block stands (water == errTotal) */
+		R.denoiseStep = 0;
+		R.opaqueAlphaError = 0;
+	}
+	FinishBlock<kD>(st, R, P, water, lo, hi, b, lane);
+	if (lane == 0)
+		next = kStepNone;
+	return true;
+}
+
+/* A pass kernel's block: runs pass S and records the next one. */
+template<int kD, int S>
+__device__ void PassStage(WarpState& st, SearchState& ss, const BlockRef& b, const LevelTables& T, const Params& P, BlockRecord& rec,
+	int& next, int lane)
+{
+	CellRegs R;
+	RestoreBlock(st, R, b, rec, P, lane);
+	RunStep<kD, S>(st, ss, R, P, T, lane);
+	const int n = NextStep(S, R, P);
+	SaveRecord(rec, R, lane);
+	if (lane == 0)
+		next = n;
+	__syncwarp();
+}
+
+/* The finish kernel's block. */
+template<int kD>
+__device__ void FinishStage(WarpState& st, const BlockRef& b, const Params& P, const BlockRecord& rec, int lane)
+{
+	CellRegs R;
+	RestoreBlock(st, R, b, rec, P, lane);
+	FinishBlock<kD>(st, R, P, rec.water, rec.startLo, rec.startHi, b, lane);
+}
+
+/* Stage STAGE of one block at queue position k; returns whether the block
+   finished (its output is written). */
+template<int kD, int STAGE>
+__device__ __forceinline__ bool StageBlock(WarpState& st, SearchState& ss, const BlockRef& b, const LevelTables& T, const Params& P,
+	const Stages& sg, int k, int lane)
+{
+	if constexpr (STAGE == kStageDraft)
+		return DraftStage<kD>(st, b, T, P, sg.rec[k], sg.next[k], lane);
+	else if constexpr (STAGE == kStepFinish)
+	{
+		FinishStage<kD>(st, b, P, sg.rec[k], lane);
+		return true;
+	}
+	else
+	{
+		PassStage<kD, STAGE>(st, ss, b, T, P, sg.rec[k], sg.next[k], lane);
+		return false;
+	}
+}
+
+/* One stage of a staged encode over the launch's queue: the draft kernel
+   takes every position; a pass or the finish kernel takes the positions
+   KStageList gathered for it.  kD as for KEncode. */
+template<int kD, int STAGE>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeStage(Job job, Stages sg, LevelTables T0, LevelTables T1)
+{
+	extern __shared__ __align__(16) unsigned char encodeSmem[];
+	const int lane = threadIdx.x & 31;
+	const int warp = threadIdx.x >> 5;
+	WarpState& st = reinterpret_cast<WarpState*>(encodeSmem)[warp];
+	SearchState& ss = reinterpret_cast<SearchState*>(encodeSmem + kWarpsPerCta * sizeof(WarpState))[warp];
+	const int n = STAGE == kStageDraft ? job.total : sg.count[STAGE < 0 ? 0 : STAGE];
+	int* counter = sg.counters + (STAGE + 1);
+	for (;;)
+	{
+		int i = 0;
+		if (lane == 0)
+			i = atomicAdd(counter, 1);
+		i = __shfl_sync(kFull, i, 0);
+		if (i >= n)
+			break;
+		const int k = STAGE == kStageDraft ? i : sg.list[i];
+		TexDesc d;
+		BlockRef b;
+		QueuedBlock(job, k, d, b);
+		const Params P = d.P;
+		bool finished;
+		if constexpr (kD == kAnyDenoise)
+		{
+			if (d.denoise)
+				finished = StageBlock<1, STAGE>(st, ss, b, T1, P, sg, k, lane);
+			else
+				finished = StageBlock<0, STAGE>(st, ss, b, T0, P, sg, k, lane);
+		}
+		else
+			finished = StageBlock<kD, STAGE>(st, ss, b, kD ? T1 : T0, P, sg, k, lane);
+		if (finished)
+			BlockFinished(d, lane);
+	}
+}
+
+/* Gathers, in queue order, the positions whose next pass is `stage` into
+   list and their number into *count (one block of 1024 threads). */
+static __global__ void __launch_bounds__(1024) KStageList(const int* next, int total, int stage, int* list, int* count)
+{
+	__shared__ int warpSums[32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	int base = 0;
+	for (int k0 = 0; k0 < total; k0 += 1024)
+	{
+		const int k = k0 + threadIdx.x;
+		const bool on = k < total && next[k] == stage;
+		const unsigned m = __ballot_sync(kFull, on);
+		if (lane == 0)
+			warpSums[warp] = __popc(m);
+		__syncthreads();
+		int before = 0, all = 0;
+		for (int w = 0; w < 32; w++)
+		{
+			const int c = warpSums[w];
+			before += w < warp ? c : 0;
+			all += c;
+		}
+		if (on)
+			list[base + before + __popc(m & ((1u << lane) - 1))] = k;
+		base += all;
+		__syncthreads();
+	}
+	if (threadIdx.x == 0)
+		*count = base;
+}
+
+/* Host-side launcher of a staged encode: the draft kernel, then for each
+   pass its list and its kernel, then the finish kernel's list and kernel.
+   The launches are capturable.  Compiled per kD in encode_*_staged.cu. */
+template<int kD>
+cudaError_t LaunchStagedEncode(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0,
+	const LevelTables& T1);
+
+/* Raises the stage kernels' dynamic shared-memory limit (once per process
+   and device, before the first launch) and reports CTAs per SM. */
+template<int kD>
+cudaError_t StagedEncodeOccupancy(int* ctasPerSm);
+
+/* Bytes of the per-position state of a staged encode of n positions
+   (records, next-pass words and the pass list; 256-byte aligned pieces),
+   after kStagedZeroed bytes of counts and queue heads that must be zero
+   before each launch. */
+constexpr size_t kStagedZeroed = 256;
+
+constexpr size_t StagedScratchBytes(int n)
+{
+	return kStagedZeroed + ((size_t(n) * sizeof(BlockRecord) + 255) & ~size_t(255)) + ((size_t(n) * 4 + 255) & ~size_t(255)) * 2;
+}
+
+/* Splits a staged scratch (256-byte aligned, StagedScratchBytes(n) bytes). */
+inline Stages SplitStaged(uint8_t* p, int n)
+{
+	Stages s;
+	s.count = (int*)p;
+	s.counters = (int*)(p + 128);
+	s.rec = (BlockRecord*)(p + kStagedZeroed);
+	uint8_t* q = p + kStagedZeroed + ((size_t(n) * sizeof(BlockRecord) + 255) & ~size_t(255));
+	s.next = (int*)q;
+	s.list = (int*)(q + ((size_t(n) * 4 + 255) & ~size_t(255)));
+	return s;
+}
+
+} // namespace nebc7

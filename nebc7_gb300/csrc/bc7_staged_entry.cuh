@@ -1,0 +1,70 @@
+/*
+ * Definitions of the staged-encode launchers declared in bc7_staged.cuh;
+ * included by the per-kDenoise translation units only.
+ */
+#pragma once
+
+#include "bc7_staged.cuh"
+
+namespace nebc7 {
+
+template<int kD, int STAGE>
+cudaError_t LaunchStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
+{
+	if (STAGE != kStageDraft)
+		KStageList<<<1, 1024, 0, stream>>>(sg.next, job.total, STAGE, sg.list, sg.count + (STAGE < 0 ? 0 : STAGE));
+	KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, T0, T1);
+	return cudaGetLastError();
+}
+
+template<int kD>
+cudaError_t LaunchStagedEncode(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0,
+	const LevelTables& T1)
+{
+	cudaError_t e = LaunchStage<kD, kStageDraft>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepRefine>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull3Mode2>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull3Mode0>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull2Mode1>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull2Mode3>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepRot5>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepRot4>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepMode7>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepMode6>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepFinish>(grid, stream, job, sg, T0, T1);
+	return e;
+}
+
+template<int kD, int STAGE>
+cudaError_t PrepareStage()
+{
+	return cudaFuncSetAttribute(KEncodeStage<kD, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(EncodeSharedBytes<true>()));
+}
+
+template<int kD>
+cudaError_t StagedEncodeOccupancy(int* ctasPerSm)
+{
+	cudaError_t e = PrepareStage<kD, kStageDraft>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepRefine>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull3Mode2>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull3Mode0>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull2Mode1>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull2Mode3>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepRot5>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepRot4>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepMode7>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepMode6>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepFinish>();
+	if (e != cudaSuccess)
+		return e;
+	/* every stage kernel has the refining kernel's shared memory and bounds */
+	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(ctasPerSm, KEncodeStage<kD, kStepFull3Mode2>, kWarpsPerCta * 32,
+		EncodeSharedBytes<true>());
+}
+
+} // namespace nebc7
+
+#define NEBC7_INSTANTIATE_STAGED(KD) \
+	template cudaError_t nebc7::LaunchStagedEncode<KD>(int, cudaStream_t, const nebc7::Job&, const nebc7::Stages&, \
+		const nebc7::LevelTables&, const nebc7::LevelTables&); \
+	template cudaError_t nebc7::StagedEncodeOccupancy<KD>(int*);

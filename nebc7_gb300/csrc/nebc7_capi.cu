@@ -8,6 +8,7 @@
  */
 #include "bc7_tables.cuh"
 #include "bc7_decode.cuh"
+#include "bc7_staged.cuh"
 #include "bc7_tools.cuh"
 
 #include "../../include/nebc7_gb300.h"
@@ -188,23 +189,36 @@ int ValidateSettings(const nebc7_settings* s)
 	return NEBC7_OK;
 }
 
-/* The encode instantiations: denoise shift x passes x code shape. */
+/* The encode instantiations: denoise shift x passes x code shape.  The
+   outlined ones also have a staged form (bc7_staged.cuh: one kernel per
+   pass), used where the launch has room for its per-block records; the
+   single kernel serves the allocation-free entry and the request loop. */
 struct EncodeVariant
 {
 	cudaError_t (*launch)(int, cudaStream_t, const Job&, const LevelTables&, const LevelTables&);
 	cudaError_t (*occupancy)(int*);
+	cudaError_t (*staged)(int, cudaStream_t, const Job&, const Stages&, const LevelTables&, const LevelTables&);
+	cudaError_t (*stagedOccupancy)(int*);
 };
 
 constexpr int kNumVariants = 6;
 constexpr int kVariantMixed = 5;   /* batches: kDenoise per texture */
 const EncodeVariant kVariants[kNumVariants] = {
-	{ LaunchEncodeKernel<0, false, kShapeCompact>, EncodeKernelOccupancy<0, false, kShapeCompact> },
-	{ LaunchEncodeKernel<0, true, kShapeOutlined>, EncodeKernelOccupancy<0, true, kShapeOutlined> },
-	{ LaunchEncodeKernel<1, false, kShapeCompact>, EncodeKernelOccupancy<1, false, kShapeCompact> },
-	{ LaunchEncodeKernel<1, true, kShapeCompact>, EncodeKernelOccupancy<1, true, kShapeCompact> },
-	{ LaunchEncodeKernel<1, true, kShapeOutlined>, EncodeKernelOccupancy<1, true, kShapeOutlined> },
-	{ LaunchEncodeKernel<kAnyDenoise, true, kShapeOutlined>, EncodeKernelOccupancy<kAnyDenoise, true, kShapeOutlined> },
+	{ LaunchEncodeKernel<0, false, kShapeCompact>, EncodeKernelOccupancy<0, false, kShapeCompact>, nullptr, nullptr },
+	{ LaunchEncodeKernel<0, true, kShapeOutlined>, EncodeKernelOccupancy<0, true, kShapeOutlined>,
+	  LaunchStagedEncode<0>, StagedEncodeOccupancy<0> },
+	{ LaunchEncodeKernel<1, false, kShapeCompact>, EncodeKernelOccupancy<1, false, kShapeCompact>, nullptr, nullptr },
+	{ LaunchEncodeKernel<1, true, kShapeCompact>, EncodeKernelOccupancy<1, true, kShapeCompact>, nullptr, nullptr },
+	{ LaunchEncodeKernel<1, true, kShapeOutlined>, EncodeKernelOccupancy<1, true, kShapeOutlined>,
+	  LaunchStagedEncode<1>, StagedEncodeOccupancy<1> },
+	{ LaunchEncodeKernel<kAnyDenoise, true, kShapeOutlined>, EncodeKernelOccupancy<kAnyDenoise, true, kShapeOutlined>,
+	  LaunchStagedEncode<kAnyDenoise>, StagedEncodeOccupancy<kAnyDenoise> },
 };
+
+bool SlotStaged(int slot)
+{
+	return kVariants[slot].staged != nullptr;
+}
 
 /* Picks the instantiation: the compact shape for the stepped default preset
    (kDenoise 1, refinement without /slow or /data), the outlined one where
@@ -251,6 +265,14 @@ int GridForSlot(int nblocks, int slot)
 			int n = 0;
 			if (kVariants[slot].occupancy(&n) != cudaSuccess)
 				return 0;
+			if (kVariants[slot].stagedOccupancy)
+			{
+				/* prepares the stage kernels too; the grid fits both forms */
+				int m = 0;
+				if (kVariants[slot].stagedOccupancy(&m) != cudaSuccess)
+					return 0;
+				n = std::min(n, m);
+			}
 			L.perSm[slot] = n > 0 ? n : 1;
 		}
 		sms = L.sms;
@@ -358,7 +380,32 @@ cudaError_t EnqueueBlockOrder(const uint8_t* bgra, long long stride, int blocksW
 	return cudaGetLastError();
 }
 
-/* Enqueues one encode.  `scratchIn` (EncodeScratchBytes bytes, 256-byte
+/* Scratch of one encode launch: the staged form adds its per-block records
+   after the EncodeScratchBytes pieces. */
+size_t LaunchScratchBytes(int nblocks, bool wantSums, const nebc7_settings& s)
+{
+	const size_t base = (EncodeScratchBytes(nblocks, wantSums) + 255) & ~size_t(255);
+	return SlotStaged(VariantSlot(s)) ? base + StagedScratchBytes(nblocks) : base;
+}
+
+/* Launches the encode of `job` with instantiation `slot`: the staged form
+   when the slot has one and `staged` (StagedScratchBytes(job.total) bytes,
+   256-byte aligned) is given, else the single kernel. */
+cudaError_t LaunchSlot(int slot, int grid, cudaStream_t stream, const Job& job, const LevelTables& T0, const LevelTables& T1,
+	uint8_t* staged)
+{
+	if (staged && kVariants[slot].staged)
+	{
+		const Stages sg = SplitStaged(staged, job.total);
+		const cudaError_t e = cudaMemsetAsync(staged, 0, kStagedZeroed, stream);
+		if (e != cudaSuccess)
+			return e;
+		return kVariants[slot].staged(grid, stream, job, sg, T0, T1);
+	}
+	return kVariants[slot].launch(grid, stream, job, T0, T1);
+}
+
+/* Enqueues one encode.  `scratchIn` (LaunchScratchBytes bytes, 256-byte
    aligned) is used when given, otherwise the scratch is taken from the
    stream-ordered allocator. */
 int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long long stride, int blocksW, int nblocks,
@@ -380,7 +427,7 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 
 	const bool wantSums = errs || ssim;
 	uint8_t* scratch = scratchIn;
-	if (!scratch && cudaMallocAsync((void**)&scratch, EncodeScratchBytes(nblocks, wantSums), stream) != cudaSuccess)
+	if (!scratch && cudaMallocAsync((void**)&scratch, LaunchScratchBytes(nblocks, wantSums, s), stream) != cudaSuccess)
 		return SetError(NEBC7_ENOMEM);
 	const EncodeScratch e = SplitScratch(scratch, nblocks, wantSums);
 	int* status = e.status;
@@ -402,7 +449,9 @@ int LaunchEncode(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, long lo
 			cudaFreeAsync(scratch, stream);
 		return SetError(NEBC7_ECUDA);
 	}
-	CK(kVariants[VariantSlot(s)].launch(grid, stream, job, *T, *T));
+	const int slot = VariantSlot(s);
+	uint8_t* staged = SlotStaged(slot) ? scratch + ((EncodeScratchBytes(nblocks, wantSums) + 255) & ~size_t(255)) : nullptr;
+	CK(LaunchSlot(slot, grid, stream, job, *T, *T, staged));
 
 	int rc = NEBC7_OK;
 	if (wantSums)
@@ -600,6 +649,7 @@ struct BatchGroup
 	int queueBase;            /* offset of its queue positions in the results */
 	int total;                /* blocks */
 	int grid;
+	long long stagedOff;      /* its staged-encode records in the batch's staged area, or -1 */
 };
 
 struct BatchSchedule
@@ -608,6 +658,7 @@ struct BatchSchedule
 	std::vector<BatchGroup> groups;
 	TexDesc* dTable = nullptr;       /* device copy */
 	cudaGraphExec_t graph = nullptr;
+	size_t stagedBytes = 0;          /* staged-encode records of all its groups */
 };
 
 } // namespace
@@ -621,6 +672,7 @@ struct nebc7_batch
 	BatchSchedule sched[2];          /* 0: one mixed launch; 1: one launch per preset group */
 	int chosen = 0;
 	uint8_t* dmem = nullptr;         /* counters, results, sums */
+	uint8_t* staged = nullptr;       /* per-group records of the staged encodes */
 	int* counters = nullptr;
 	BlockResult* results = nullptr;
 	long long* errs = nullptr;
@@ -672,6 +724,7 @@ void BuildSchedule(nebc7_batch* b, int which)
 			g.queueBase = queue;
 			g.total = 0;
 			g.grid = 0;
+			g.stagedOff = -1;
 			S.groups.push_back(g);
 		}
 		BatchGroup& g = S.groups.back();
@@ -694,8 +747,18 @@ void BuildSchedule(nebc7_batch* b, int which)
 		g.total += d.nblocks;
 		queue += d.nblocks;
 	}
+	long long off = 0;
 	for (BatchGroup& g : S.groups)
+	{
 		g.grid = GridForSlot(g.total, g.slot);
+		g.stagedOff = -1;
+		if (SlotStaged(g.slot) && g.total > 0)
+		{
+			g.stagedOff = off;
+			off += (long long)((StagedScratchBytes(g.total) + 255) & ~size_t(255));
+		}
+	}
+	S.stagedBytes = size_t(off);
 }
 
 /* Enqueues schedule `which` on stream st (capturable): clears the outputs
@@ -730,7 +793,7 @@ int EnqueueSchedule(nebc7_batch* b, int which, cudaStream_t st)
 		job.order = nullptr;
 		job.single = S.table[G.firstTex];
 		const cudaStream_t gs = g == 0 ? st : b->side[g - 1];
-		CK(kVariants[G.slot].launch(G.grid, gs, job, *b->T[0], *b->T[1]));
+		CK(LaunchSlot(G.slot, G.grid, gs, job, *b->T[0], *b->T[1], G.stagedOff >= 0 ? b->staged + G.stagedOff : nullptr));
 	}
 	if (ng > 1)
 	{
@@ -799,6 +862,7 @@ void FreeBatch(nebc7_batch* b)
 	if (b->cap)
 		cudaStreamDestroy(b->cap);
 	cudaFree(b->dmem);
+	cudaFree(b->staged);
 	delete b;
 }
 
@@ -822,6 +886,8 @@ struct ServerRequest
 	nebc7_settings settings;
 	uint8_t* dst;
 	double tSubmit = 0, tLaunch = 0, tDone = 0;
+	int slot = -1;               /* the launch slot that ran it */
+	long long launch = -1;       /* the server's launch sequence number */
 	int state = 0;               /* 0 queued, 1 admitted, 2 on the device, 3 done, < 0 error code */
 	size_t off = 0, bytes = 0;   /* its part of the arena */
 	int64_t errs[2] = { 0, 0 };
@@ -917,6 +983,7 @@ struct nebc7_server
 	bool stop = false;
 	const LevelTables* T[2] = { nullptr, nullptr };
 	long long launches = 0, completed = 0, failed = 0;
+	double t0 = 0;                    /* creation time, origin of the request times */
 };
 
 namespace {
@@ -1126,8 +1193,11 @@ void ServerLoop(nebc7_server* sv)
 			const double now = NowSeconds();
 			for (int64_t id : batch)
 			{
-				sv->reqs[id].state = 2;
-				sv->reqs[id].tLaunch = now;
+				ServerRequest& r = sv->reqs[id];
+				r.state = 2;
+				r.tLaunch = now;
+				r.slot = int(&slot - sv->slots.data());
+				r.launch = sv->launches;
 			}
 			const int rc = LaunchServerBatch(sv, slot, batch);
 			if (rc != NEBC7_OK)
@@ -1392,7 +1462,7 @@ int nebc7_encode_host(uint8_t* dst, const uint8_t* bgra, const uint8_t* mask, lo
 	const size_t offImg = Align256(nb * 16);
 	const size_t offMask = offImg + Align256(img);
 	const size_t offScratch = offMask + (mask ? Align256(img) : 0);
-	if (!ReserveSlot(slot, offScratch + EncodeScratchBytes(int(nb), true)))
+	if (!ReserveSlot(slot, offScratch + LaunchScratchBytes(int(nb), true, *settings)))
 	{
 		ReleaseSlot(slot);
 		return SetError(NEBC7_ENOMEM);
@@ -1549,7 +1619,9 @@ int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_ba
 		const size_t offRes = 256 + ((sizeof(int) * 2 * ng + 255) & ~size_t(255));
 		const size_t offErr = offRes + ((size_t(total) * sizeof(BlockResult) + 255) & ~size_t(255));
 		const size_t bytes = offErr + size_t(n) * 4 * sizeof(long long);
-		if (cudaMalloc((void**)&b->dmem, bytes) != cudaSuccess)
+		const size_t stagedBytes = std::max(b->sched[0].stagedBytes, b->sched[1].stagedBytes);
+		if (cudaMalloc((void**)&b->dmem, bytes) != cudaSuccess ||
+			(stagedBytes && cudaMalloc((void**)&b->staged, stagedBytes) != cudaSuccess))
 			rc = SetError(NEBC7_ENOMEM);
 		else
 		{
@@ -1735,6 +1807,7 @@ int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out)
 	*out = nullptr;
 	nebc7_server* sv = new nebc7_server;
 	sv->cfg = *cfg;
+	sv->t0 = NowSeconds();
 	int rc = NEBC7_OK;
 	if (cudaGetDevice(&sv->device) != cudaSuccess)
 		rc = SetError(NEBC7_ECUDA);
@@ -1841,6 +1914,11 @@ int nebc7_server_wait(nebc7_server* sv, int64_t ticket, double timeout_s, nebc7_
 		info->status = rc;
 		info->queue_ms = (r.tLaunch - r.tSubmit) * 1e3;
 		info->latency_ms = (r.tDone - r.tSubmit) * 1e3;
+		info->submit_at_ms = (r.tSubmit - sv->t0) * 1e3;
+		info->launch_at_ms = (r.tLaunch - sv->t0) * 1e3;
+		info->done_at_ms = (r.tDone - sv->t0) * 1e3;
+		info->slot = r.slot;
+		info->launch = r.launch;
 		info->errs[0] = r.errs[0];
 		info->errs[1] = r.errs[1];
 		info->ssim[0] = r.ssim[0];

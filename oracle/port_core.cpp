@@ -774,8 +774,9 @@ void ChannelLevels(const Config& cfg, Levels& L, const Area& area, int offset, i
 	const uint32_t top16 = uint32_t(top) & 0xFFFF;
 
 	PORT_COUNT(kScanCalls, 1);
+	uint64_t scanned = 0;   /* window cells scored (work counters only) */
 	auto sumAt = [&](int32_t c) -> uint32_t {
-		PORT_COUNT(kScanTerms, count);
+		scanned++;
 		uint32_t s = 0;
 		for (uint32_t i = 0; i < count; i++)
 		{
@@ -821,6 +822,7 @@ void ChannelLevels(const Config& cfg, Levels& L, const Area& area, int offset, i
 			L.e[0].err = e;
 			L.e[0].color = DecodeColor(bestKey & 0xFFFFu, shift, reverse);
 		}
+		PORT_COUNT(kScanTerms, scanned * count);
 		return;
 	}
 
@@ -876,6 +878,8 @@ void ChannelLevels(const Config& cfg, Levels& L, const Area& area, int offset, i
 		}
 	}
 
+	PORT_COUNT(kScanTerms, scanned * count);
+	(void)scanned;
 	KeepSmallest(cfg, L, keys, n, weight, shift, reverse, maxSize);
 }
 
@@ -950,6 +954,7 @@ void ChannelLevelsHalf(const Config& cfg, Levels& L, const Area& area, int offse
 	const int pL = reverse ? (pbits >> 8) : (pbits & 1);
 
 	PORT_COUNT(kScanCalls, 1);
+	uint64_t scanned = 0;   /* window cells scored (work counters only) */
 	for (int32_t iH = win.HL + pH; iH < win.HH; iH += 2)
 	{
 		const int32_t cH = iH << shift;
@@ -963,7 +968,7 @@ void ChannelLevelsHalf(const Config& cfg, Levels& L, const Area& area, int offse
 				if (!((flags >> (2 * j)) & 1))
 					continue;
 				const int32_t cc = c + pL + 2 * j;
-				PORT_COUNT(kScanTerms, count);
+				scanned++;
 				int32_t s = 0;
 				for (uint32_t i = 0; i < count; i++)
 				{
@@ -980,6 +985,8 @@ void ChannelLevelsHalf(const Config& cfg, Levels& L, const Area& area, int offse
 		}
 	}
 
+	PORT_COUNT(kScanTerms, scanned * count);
+	(void)scanned;
 	KeepSmallest(cfg, L, keys, n, weight, shift, reverse, maxSize);
 }
 
@@ -1035,12 +1042,13 @@ int EstimateChannelLevels(const Config& cfg, const Area& area, int offset, int w
 	/* rows[iH]: saturating sum of the cut (row-minimum squared) values,
 	   a lower bound for every candidate of row iH (:233-251). */
 	PORT_COUNT(kEstCalls, 1);
+	uint64_t terms = 0;   /* (cell or row, pixel) terms (work counters only) */
 	uint32_t rows[256];
 	for (int32_t iH = win.HL & ~15; iH < win.HH; iH++)
 	{
 		if (iH < 0)
 			continue;
-		PORT_COUNT(kEstTerms, count);
+		terms += count;
 		uint32_t s = 0;
 		for (uint32_t i = 0; i < count; i++)
 			s += cuts[i][iH];
@@ -1056,7 +1064,7 @@ int EstimateChannelLevels(const Config& cfg, const Area& area, int offset, int w
 		uint32_t rowBest = 0xFFFF;
 		for (int32_t iL = cH, hL = std::min(win.LH, iH) + cH; iL <= hL; iL += 32)
 		{
-			PORT_COUNT(kEstTerms, 32 * count);
+			terms += 32 * count;
 			for (int j = 0; j < 32; j++)
 			{
 				uint32_t s = 0;
@@ -1071,6 +1079,8 @@ int EstimateChannelLevels(const Config& cfg, const Area& area, int offset, int w
 		}
 		best = std::min(best, int32_t(rowBest));
 	}
+	PORT_COUNT(kEstTerms, terms);
+	(void)terms;
 	return best * weight;
 }
 

@@ -106,3 +106,33 @@ def test_server_rejects_requests_beyond_its_budget(native):
         srv.submit(img, None, dst, Settings(*PRESETS["draft"]))
     assert e.value.code == 6
     srv.close()
+
+
+def test_server_admits_requests_while_others_run(native):
+    """Continuous batching: requests that arrive while a long launch is on
+    the device start on another slot and come back before it ends, with the
+    blocks a plain encode gives them."""
+    import time
+    from nebc7_gb300 import Server
+    from nebc7_gb300._native import Settings
+    big = synth.image_for("photo_like", 1024, 512, 21)
+    small = _requests(6, 22)
+    srv = Server(hbm_budget=256 << 20, max_batch=4, streams=2)
+    big_out = np.zeros(((512 // 4) * (1024 // 4), 16), np.uint8)
+    t_big = srv.submit(big, None, big_out, Settings(*PRESETS["precise"]))
+    time.sleep(0.005)
+    outs, tickets = [], []
+    for img, mask, preset in small:
+        h, w = img.shape[:2]
+        outs.append(np.zeros(((h // 4) * (w // 4), 16), np.uint8))
+        tickets.append(srv.submit(img, mask, outs[-1], Settings(*PRESETS[preset])))
+    infos = [srv.wait(t) for t in tickets]
+    b = srv.wait(t_big)
+    srv.close()
+    joined = [s for s in infos
+              if s["submit_at_ms"] > b["launch_at_ms"] and s["launch_at_ms"] < b["done_at_ms"]
+              and s["done_at_ms"] < b["done_at_ms"] and s["slot"] != b["slot"] and s["launch"] != b["launch"]]
+    assert joined, (b, infos)
+    assert np.array_equal(big_out, _plain(native, big, None, "precise")[0])
+    for i, (img, mask, preset) in enumerate(small):
+        assert np.array_equal(outs[i], _plain(native, img, mask, preset)[0])
