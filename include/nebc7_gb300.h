@@ -146,15 +146,19 @@ int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
 /* Builds the level tables of `denoise` on the current device ahead of use. */
 int nebc7_init_device(int denoise);
 
-/* Copies level table `which` (0..13, in the order d2v8, d2v7, d2v6, d2v5,
-   c2v8, c2v6, c2v5, d3v7s, d3v6, d3v5, c3v7s, c3v5, d4h, d2h) of `denoise`
+/* Copies level table `which` (0..14, in the order d2v8, d2v7, d2v6, d2v5,
+   c2v8, c2v6, c2v5, d3v7s, d3v6, d3v5, c3v7s, c3v5, d4h, d2h, d3v8) of `denoise`
    from the current device to `host`, building the tables first if needed.
    *bytes receives the table's size; NEBC7_ETOOBIG when `capacity` is
    smaller.  The reference's tables are process globals filled by
    InitLevels (src/Bc7Tables.cpp:583-777); this read-back lets a caller
    compare the device-built copies with them entry by entry.  d2v8, d4h and
    d2h are stored by endpoint differences here: [cH - x + 255][cL - x + 255],
-   511 rows of 512 bytes or of 256 bytes of packed nibbles. */
+   511 rows of 512 bytes or of 256 bytes of packed nibbles.  d3v8 has no
+   reference counterpart: the byte table of 3-bit indices with 8-bit
+   endpoints, by differences, which the encoder reads in place of the
+   reference's reduced tables of 3-bit indices (their entries at the
+   bit-replicated endpoints). */
 int nebc7_table_read(int denoise, int which, void* host, long long capacity, long long* bytes);
 
 /* Allocation-free variant of nebc7_encode_device (no counterpart in the

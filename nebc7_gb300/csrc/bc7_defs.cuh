@@ -96,6 +96,7 @@ struct LevelTables
 	const uint16_t* c3v5;  /* [256][32]      */
 	const uint8_t* d4h;    /* [511][256] nibbles, by differences (HalfAt) */
 	const uint8_t* d2h;    /* [511][256] nibbles, by differences (HalfAt) */
+	const uint8_t* d3v8;   /* [511][512] bytes of 3-bit indices, by differences (DiffAt) */
 };
 
 /* Per-launch encoder settings: the reference's InitTables flags

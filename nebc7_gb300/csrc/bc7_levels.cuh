@@ -37,6 +37,26 @@ __device__ __forceinline__ int Wadd(int a, int b) { return int(unsigned(a) + uns
 __device__ __forceinline__ int Wsub(int a, int b) { return int(unsigned(a) - unsigned(b)); }
 __device__ __forceinline__ unsigned Shr32(unsigned v, unsigned s) { return v >> (s & 31); }
 
+/* A reduced table's s-bit endpoint expanded to 8 bits by bit replication. */
+__device__ __forceinline__ int ExpandTo8(int v, int s)
+{
+	return s >= 8 ? v : ((v << (8 - s)) | (v >> (2 * s - 8)));
+}
+
+/* The reduced tables of s-bit endpoints hold, for every x, the 8-bit
+   table's entry at the expanded endpoints; the 8-bit byte tables of 2- and
+   3-bit indices are stored by endpoint differences (DiffAt).  For
+   candidate cc (endpoints cc >> s, cc & (2^s - 1)) the difference-table
+   entry of channel value x is table[DiffBase(cc, s) - 513 x]: one lookup
+   per term, as in the per-x layout, but in a region near the table's
+   diagonal that every block shares, where the per-x rows of the distinct
+   values of a channel lie far apart. */
+__device__ __forceinline__ int DiffBase(int cc, int s)
+{
+	const int eH = ExpandTo8(cc >> s, s), eL = ExpandTo8(cc & ((1 << s) - 1), s);
+	return (eH << 9) + eL + 255 * 513;
+}
+
 /* d with d*d < top (src/SnippetLevelsBuffer.h:78-88): truncated single
    precision square root, NaN (negative top) giving INT_MIN. */
 template<int kD>
@@ -160,7 +180,7 @@ __device__ __forceinline__ ChanList ZeroList(int2* nodes, int color, int lane)
 /* LevelsBuffer and LevelsBufferHalf: writes up to maxSize nodes (err, color). */
 template<int kD, bool HALF>
 __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight,
-	int water, int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int* uniq, int lane)
+	int water, int bits, int pbits, bool transparent, const uint8_t* table, bool byDiff, int maxSize, int* uniq, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
 	const int shift = bits + int(pbits >= 0 || HALF);
@@ -204,7 +224,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	/* byte tables by (x, c); with 8-bit endpoints (shift 8) the byte table
 	   goes by DiffAt and the half tables by HalfAt */
 	const int rowSize = 1 << (2 * shift);
-	const bool diff = shift == 8;
+	const bool diff = shift == 8 || byDiff;
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 	const bool pvar = HALF || pbits >= 0;
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
@@ -254,6 +274,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 			unsigned key = 0xFFFFFFFFu;
 			if (on)
 			{
+				const int dbase = DiffBase(cc, shift);
 				/* four distinct values per step, their table reads in flight
 				   together (unsigned sums do not depend on the order) */
 				auto term = [&](int e) {
@@ -262,7 +283,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 					if (HALF)
 						v = HalfAt(table, x, cc & 0xFF, cc >> 8);
 					else if (diff)
-						v = DiffAt(table, x, cc & 0xFF, cc >> 8);
+						v = table[dbase - 513 * x];
 					else
 						v = table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
@@ -306,16 +327,17 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
    refinement (the common case of the default preset) inlines the scan. */
 template<int kD, bool HALF>
 __device__ NEBC7_SHARED ChanList ChannelLevels(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
-	int bits, int pbits, bool transparent, const uint8_t* table, int maxSize, int* uniq, int lane)
+	int bits, int pbits, bool transparent, const uint8_t* table, bool byDiff, int maxSize, int* uniq, int lane)
 {
-	return ChannelLevelsScan<kD, HALF>(nodes, ar, ai, offset, weight, water, bits, pbits, transparent, table, maxSize, uniq, lane);
+	return ChannelLevelsScan<kD, HALF>(nodes, ar, ai, offset, weight, water, bits, pbits, transparent, table, byDiff, maxSize, uniq,
+		lane);
 }
 
 /* Single best candidate over the narrower window of the alpha slot of modes
    4 and 5 (src/SnippetLevelsBuffer.h:148-188, 433-490). */
 template<int kD>
 __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar, const AreaInfo& ai, int offset, int weight, int water,
-	int bits, bool transparent, const uint8_t* table, int* uniq, int lane)
+	int bits, bool transparent, const uint8_t* table, bool byDiff, int* uniq, int lane)
 {
 	ChanList res{ MaxColorError<kD>() * 2, 0 };
 	const int shift = bits;
@@ -336,7 +358,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 		top = 0xFFFF;
 	const unsigned top16 = unsigned(top) & 0xFFFF;
 	const int rowSize = 1 << (2 * shift);
-	const bool diff = shift == 8;   /* the 8-bit byte table goes by DiffAt */
+	const bool diff = shift == 8 || byDiff;   /* DiffBase */
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
 	unsigned best = 0xFFFFFFFFu;
@@ -358,9 +380,10 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 				break;
 			if (chunkOn && ((mask >> (2 * j)) & 1))
 			{
+				const int dbase = DiffBase(cc, shift);
 				auto term = [&](int e) {
 					const int x = e & 0xFFFF;
-					const unsigned v = diff ? DiffAt(table, x, cc & 0xFF, cc >> 8) : table[size_t(x) * rowSize + cc];
+					const unsigned v = diff ? table[dbase - 513 * x] : table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
 				};
 				unsigned s = 0;
@@ -395,7 +418,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
    are visited in order with the running best. */
 template<int kD>
 __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo& ai, int offset, int weight, int water, int bits,
-	bool transparent, const uint8_t* table, const uint16_t* tower, int* uniq, int lane)
+	bool transparent, const uint8_t* table, bool byDiff, const uint16_t* tower, int* uniq, int lane)
 {
 	const int shift = bits;
 	const int count = transparent ? ai.active : ai.count;
@@ -417,7 +440,7 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 	if (top > 0xFFFF)
 		top = 0xFFFF;
 	const int rowSize = 1 << (2 * bits);
-	const bool diff = bits == 8;   /* the 8-bit byte table goes by DiffAt */
+	const bool diff = bits == 8 || byDiff;   /* DiffBase */
 	const int towerSize = 1 << bits;
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
@@ -451,9 +474,10 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 			{
 				/* cc = iL + lane stays in row iH (iL <= hL, iL - cH a multiple of 32) */
 				const int cc = iL + lane;
+				const int dbase = DiffBase(cc, bits);
 				auto term = [&](int e) {
 					const int x = e & 0xFFFF;
-					const unsigned v = diff ? DiffAt(table, x, cc & 0xFF, cc >> 8) : table[size_t(x) * rowSize + cc];
+					const unsigned v = diff ? table[dbase - 513 * x] : table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
 				};
 				unsigned s = 0;

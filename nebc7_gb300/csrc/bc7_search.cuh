@@ -273,22 +273,24 @@ __device__ NEBC7_SHARED int TryVariants3(const Area& ar, const AreaInfo& ai, con
 struct Spec3
 {
 	int bits;               /* candidate list bits */
-	const uint8_t* table;
+	const uint8_t* table;   /* by differences (DiffBase) unless it is the shared-p-bit table */
+	bool byDiff;
 	int estBits;
-	const uint8_t* estTable;
 	const uint16_t* estTower;
 };
 
 template<int MODE>
 __device__ __forceinline__ Spec3 GetSpec3(const LevelTables& T)
 {
+	/* mode 1's shared p-bit table marks endpoint pairs of different parity
+	   (0xFF), which its estimates read: it stays in the per-x layout */
 	if (MODE == 0)
-		return Spec3{ 4, T.d3v5, 5, T.d3v5, T.c3v5 };
+		return Spec3{ 4, T.d3v8, true, 5, T.c3v5 };
 	if (MODE == 1)
-		return Spec3{ 6, T.d3v7s, 7, T.d3v7s, T.c3v7s };
+		return Spec3{ 6, T.d3v7s, false, 7, T.c3v7s };
 	if (MODE == 2)
-		return Spec3{ 5, T.d2v5, 5, T.d2v5, T.c2v5 };
-	return Spec3{ 7, T.d2v8, 8, T.d2v8, T.c2v8 };
+		return Spec3{ 5, T.d2v8, true, 5, T.c2v5 };
+	return Spec3{ 7, T.d2v8, true, 8, T.c2v8 };
 }
 
 template<int MODE>
@@ -308,15 +310,18 @@ __device__ NEBC7_PASS bool InitLevels3(SearchState& ss, int v, const Area& ar, c
 	int water, const int est[3], ChanList cl[3], int lane)
 {
 	const int pb = Pbits(MODE, v);
-	cl[0] = ChannelLevels<kD, false>(ss.lists[v][0], ar, ai, 1, P.wG, water - est[1] - est[2], sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
+	cl[0] = ChannelLevels<kD, false>(ss.lists[v][0], ar, ai, 1, P.wG, water - est[1] - est[2], sp.bits, pb, false, sp.table, sp.byDiff, 32,
+		ss.uniq, lane);
 	const int min1 = cl[0].minErr;
 	if (min1 >= water)
 		return false;
-	cl[1] = ChannelLevels<kD, false>(ss.lists[v][1], ar, ai, 2, P.wR, water - min1 - est[2], sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
+	cl[1] = ChannelLevels<kD, false>(ss.lists[v][1], ar, ai, 2, P.wR, water - min1 - est[2], sp.bits, pb, false, sp.table, sp.byDiff, 32,
+		ss.uniq, lane);
 	const int min2 = cl[1].minErr;
 	if (min1 + min2 >= water)
 		return false;
-	cl[2] = ChannelLevels<kD, false>(ss.lists[v][2], ar, ai, 3, P.wB, water - min1 - min2, sp.bits, pb, false, sp.table, 32, ss.uniq, lane);
+	cl[2] = ChannelLevels<kD, false>(ss.lists[v][2], ar, ai, 3, P.wB, water - min1 - min2, sp.bits, pb, false, sp.table, sp.byDiff, 32,
+		ss.uniq, lane);
 	return min1 + min2 + cl[2].minErr < water;
 }
 
@@ -405,17 +410,17 @@ __device__ NEBC7_PASS int EstimateLevels3(SearchState& ss, const Area& ar, const
 	int error = 0;
 	if (error < water)
 	{
-		const int l1 = EstimateChannelLevels<kD>(ar, ai, 1, P.wG, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
+		const int l1 = EstimateChannelLevels<kD>(ar, ai, 1, P.wG, water - error, sp.estBits, false, sp.table, sp.byDiff, sp.estTower, ss.uniq, lane);
 		est[1] = l1;
 		error += l1;
 		if (error < water)
 		{
-			const int l2 = EstimateChannelLevels<kD>(ar, ai, 2, P.wR, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
+			const int l2 = EstimateChannelLevels<kD>(ar, ai, 2, P.wR, water - error, sp.estBits, false, sp.table, sp.byDiff, sp.estTower, ss.uniq, lane);
 			est[2] = l2;
 			error += l2;
 			if (error < water)
 			{
-				const int l3 = EstimateChannelLevels<kD>(ar, ai, 3, P.wB, water - error, sp.estBits, false, sp.estTable, sp.estTower, ss.uniq, lane);
+				const int l3 = EstimateChannelLevels<kD>(ar, ai, 3, P.wB, water - error, sp.estBits, false, sp.table, sp.byDiff, sp.estTower, ss.uniq, lane);
 				est[3] = l3;
 				error += l3;
 				if (error < water)
@@ -740,15 +745,18 @@ __device__ NEBC7_PASS bool InitLevels4(SearchState& ss, int v, int pbits, const 
 		}
 		else if (MODE == 6)
 		{
-			cl[c] = ChannelLevels<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d4h, 20, ss.uniq, lane);
+			cl[c] = ChannelLevels<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d4h, true, 20, ss.uniq,
+				lane);
 		}
 		else if (MODE == 9)
 		{
-			cl[c] = ChannelLevelsScan<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, 20, ss.uniq, lane);
+			cl[c] = ChannelLevelsScan<kD, true>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 7, pbits, c != 0, T.d2h, true, 20,
+				ss.uniq, lane);
 		}
 		else
 		{
-			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, T.d2v6, 20, ss.uniq, lane);
+			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, T.d2v8, true, 20,
+				ss.uniq, lane);
 		}
 		used += cl[c].minErr;
 		if (used >= water)
@@ -887,7 +895,7 @@ __device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const
 		}
 		if (!ai.opaque)
 		{
-			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, T.d2v6, T.c2v6, ss.uniq, lane);
+			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, T.d2v8, true, T.c2v6, ss.uniq, lane);
 			est[0] = l0;
 			error += l0;
 		}
@@ -898,7 +906,7 @@ __device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const
 		{
 			if (!(error < water))
 				return water;
-			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, T.d2v6, T.c2v6, ss.uniq, lane);
+			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, T.d2v8, true, T.c2v6, ss.uniq, lane);
 			est[c] = l;
 			error += l;
 		}
@@ -1075,14 +1083,14 @@ __device__ NEBC7_PASS int CompressRotSubset(WarpState& st, SearchState& ss, cons
 	{
 		cbits = 5;
 		abits = 6;
-		ctab = idx32 ? T.d3v5 : T.d2v5;
-		atab = idx32 ? T.d2v6 : T.d3v6;
+		ctab = idx32 ? T.d3v8 : T.d2v8;
+		atab = idx32 ? T.d2v8 : T.d3v8;
 	}
 	else
 	{
 		cbits = 7;
 		abits = 8;
-		ctab = T.d2v7;
+		ctab = T.d2v8;
 		atab = T.d2v8;
 	}
 	const int wts[4] = { P.wA, P.wG, P.wR, P.wB };
@@ -1093,9 +1101,9 @@ __device__ NEBC7_PASS int CompressRotSubset(WarpState& st, SearchState& ss, cons
 		if (c == 0 && ai.opaque)
 			cl[0] = ZeroList(ss.lists[0][0], 0xFFFF, lane);
 		else if (c == a)
-			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, ss.uniq, lane);
+			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, true, ss.uniq, lane);
 		else
-			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, 32, ss.uniq, lane);
+			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, true, 32, ss.uniq, lane);
 		used += cl[c].minErr;
 		if (used >= water)
 			return water;

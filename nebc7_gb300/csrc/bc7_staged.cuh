@@ -3,11 +3,13 @@
  * time goes to the full searches (precise, /slow, /data, mixed batches).
  *
  * The per-block pipeline of src/Bc7Core.cpp:1516-1823 runs as a sequence of
- * persistent kernels instead of one: the draft chain, then one kernel per
- * refinement / full-search pass of the normal and slow chains
- * (src/Bc7Core.cpp:1604-1745), then the final pack, self-check and quality
- * sums.  Every kernel holds the code of one pass only, so the warps of an SM
- * run the same few kilobytes of instructions; in a single kernel whose warps
+ * persistent kernels instead of one: the start of the draft chain (the
+ * starting block, the Mode6Index2 and mode 6 fast passes), the rest of the
+ * draft chain in four kernels, one kernel per refinement / full-search pass
+ * of the normal and slow chains (src/Bc7Core.cpp:1604-1745), then the final
+ * pack, self-check and quality sums.  Every kernel holds the code of one or
+ * two passes, so the warps of an SM run the same few kilobytes of
+ * instructions; in a single kernel whose warps
  * sit in different passes the instruction working set outgrows the
  * instruction cache and most issue slots are lost to instruction fetch.
  *
@@ -26,10 +28,15 @@
 
 namespace nebc7 {
 
-/* The passes after the draft chain, in chain order; kStepFinish packs. */
+/* The passes after the first kernel, in chain order: the rest of the draft
+   chain, then the normal and slow chains; kStepFinish packs. */
 enum StageStep
 {
-	kStepRefine = 0,
+	kStepDraftRot = 0,     /* fast passes of modes 4 and 5 */
+	kStepDraftMode7,       /* fast pass of mode 7 */
+	kStepDraftOpaque31,    /* fast passes of the opaque modes 3 and 1 */
+	kStepDraftOpaque20,    /* fast passes of the opaque modes 2 and 0 */
+	kStepRefine,
 	kStepFull3Mode2,
 	kStepFull3Mode0,
 	kStepFull2Mode1,
@@ -43,7 +50,7 @@ enum StageStep
 };
 
 constexpr int kStageDraft = -1;
-constexpr int kStepNone = -1;   /* finished in the draft kernel */
+constexpr int kStepNone = -1;   /* finished in the first kernel (an exact starting block) */
 
 /* A block's Cell scalars between pass kernels. */
 struct __align__(16) BlockRecord
@@ -106,11 +113,34 @@ __device__ __forceinline__ void RestoreBlock(WarpState& st, CellRegs& R, const B
 	BuildAreaList(st.area1, st, R, 0xFFFF, 0, lane);
 }
 
-/* One pass of the normal / slow chains (the bodies of NormalPasses). */
+/* One stage: passes of the draft chain after the mode 6 fast pass
+   (DraftChain), or one pass of the normal / slow chains (NormalPasses). */
 template<int kD, int S>
 __device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
-	if constexpr (S == kStepRefine)
+	if constexpr (S == kStepDraftRot)
+	{
+		/* entered with errTotal > step (src/Bc7Core.cpp:1558-1566) */
+		FastRot<kD, 4>(st, R, P, lane);
+		if (R.errTotal > R.denoiseStep)
+			FastRot<kD, 5>(st, R, P, lane);
+	}
+	else if constexpr (S == kStepDraftMode7)
+		FastMode7<kD>(st, R, P, T, lane);
+	else if constexpr (S == kStepDraftOpaque31)
+	{
+		/* entered with errTotal > OA + step (src/Bc7Core.cpp:1577-1585) */
+		FastOpaque<kD, 3>(st, R, P, lane);
+		if (R.errTotal > R.opaqueAlphaError + R.denoiseStep)
+			FastOpaque<kD, 1>(st, R, P, lane);
+	}
+	else if constexpr (S == kStepDraftOpaque20)
+	{
+		FastOpaque<kD, 2>(st, R, P, lane);
+		if (R.errTotal > R.opaqueAlphaError + R.denoiseStep)
+			FastOpaque<kD, 0>(st, R, P, lane);
+	}
+	else if constexpr (S == kStepRefine)
 	{
 		const int OA = R.opaqueAlphaError;
 		switch (R.bestMode)
@@ -146,12 +176,32 @@ __device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs
 		FullMode6<kD>(st, ss, R, P, T, lane);
 }
 
-/* The pass after S: the nesting of the normal and slow chains in
-   NormalPasses (src/Bc7Core.cpp:1677-1745), whose conditions are tested
-   when each pass is reached. */
+/* The draft chain's opaque passes run for blocks whose alpha stays above
+   239 (src/Bc7Core.cpp:1577), after the transparent chain however far it
+   went; then the normal passes, or the pack. */
+__device__ __forceinline__ int AfterTransparentChain(const CellRegs& R, const Params& P)
+{
+	if (int(int16_t(R.a1.minmax[0])) > 255 - 16 && R.errTotal > R.opaqueAlphaError + R.denoiseStep)
+		return kStepDraftOpaque31;
+	return (P.doNormal && P.doDraft != 2) ? kStepRefine : kStepFinish;
+}
+
+/* The pass after S: the nesting of the draft chain (src/Bc7Core.cpp:
+   1546-1597, DraftChain) and of the normal and slow chains in NormalPasses
+   (src/Bc7Core.cpp:1677-1745), whose conditions are tested when each pass
+   is reached. */
 __device__ __forceinline__ int NextStep(int S, const CellRegs& R, const Params& P)
 {
 	const int OA = R.opaqueAlphaError, step = R.denoiseStep, e = R.errTotal;
+	const int afterDraft = (P.doNormal && P.doDraft != 2) ? kStepRefine : kStepFinish;
+	switch (S)
+	{
+	case kStepDraftRot: return e > step ? kStepDraftMode7 : AfterTransparentChain(R, P);
+	case kStepDraftMode7: return AfterTransparentChain(R, P);
+	case kStepDraftOpaque31: return e > OA + step ? kStepDraftOpaque20 : afterDraft;
+	case kStepDraftOpaque20: return afterDraft;
+	default: break;
+	}
 	if (R.a1.opaque)
 	{
 		switch (S)
@@ -222,9 +272,11 @@ __device__ __forceinline__ void FinishBlock(WarpState& st, CellRegs& R, const Pa
 	StoreBlock<kD>(b, R, lo, hi, qa, qc, lane);
 }
 
-/* The draft kernel's block: EncodeBlockAt up to the normal passes.  A block
-   that goes on to them saves its record and waits; the others finish here.
-   Returns whether the block finished. */
+/* The first kernel's block: the start of EncodeBlockAt and of the draft
+   chain (src/Bc7Core.cpp:1516-1556: the starting block, its error, the
+   stepping values, the Mode6Index2 and mode 6 fast passes).  An exact
+   starting block is written at once; every other block saves its record
+   for the next stage and waits.  Returns whether the block finished. */
 template<int kD>
 __device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& T, const Params& P, BlockRecord& rec, int& next,
 	int lane)
@@ -254,7 +306,8 @@ __device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& 
 	BuildAreaList(st.area1, st, R, 0xFFFF, 0, lane);
 	R.personalMode = -1;
 	R.personalParam = -1;
-	int water = R.errTotal;
+	const int water = R.errTotal;
+	int n = kStepFinish;
 	if (P.doDraft)
 	{
 		const int step = R.a1.active * ((P.denoiseStep * (R.a1.opaque ? P.wColor : P.wColorAlpha)) >> (kD + kD));
@@ -271,20 +324,28 @@ __device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& 
 			e = int(__reduce_add_sync(kFull, unsigned(e)));
 			R.opaqueAlphaError = R.a1.opaque ? 0 : e * P.wA;
 		}
-		water = R.errTotal;
-		DraftChain<kD>(st, R, P, T, lane);
-		if (P.doNormal && P.doDraft != 2)
+		if (P.doDraft == 2)
 		{
-			SaveRecord(rec, R, lane);
-			if (lane == 0)
+			/* the "Mode6Index2 fast" run: the draft chain reduced to its
+			   first pass (no counterpart in the reference) */
+			if (R.errTotal > step && (kD > 0 || P.denoiseStep > 0))
+				FastMode6<kD, true>(st, R, P, T);
+		}
+		else
+		{
+			if (R.errTotal > step)
 			{
-				rec.startLo = lo;
-				rec.startHi = hi;
-				rec.water = water;
-				next = kStepRefine;
+				if (kD > 0 || P.denoiseStep > 0)
+					FastMode6<kD, true>(st, R, P, T);
+				if (R.errTotal > step)
+				{
+					FastMode6<kD, false>(st, R, P, T);
+					if (R.errTotal > step)
+						n = kStepDraftRot;
+				}
 			}
-			__syncwarp();
-			return false;
+			if (n != kStepDraftRot)
+				n = AfterTransparentChain(R, P);
 		}
 	}
 	else
@@ -293,10 +354,16 @@ __device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& 
 		R.denoiseStep = 0;
 		R.opaqueAlphaError = 0;
 	}
-	FinishBlock<kD>(st, R, P, water, lo, hi, b, lane);
+	SaveRecord(rec, R, lane);
 	if (lane == 0)
-		next = kStepNone;
-	return true;
+	{
+		rec.startLo = lo;
+		rec.startHi = hi;
+		rec.water = water;
+		next = n;
+	}
+	__syncwarp();
+	return false;
 }
 
 /* A pass kernel's block: runs pass S and records the next one. */
@@ -385,19 +452,33 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeStage(Job job, St
 }
 
 /* Gathers, in queue order, the positions whose next pass is `stage` into
-   list and their number into *count (one block of 1024 threads). */
+   list and their number into *count (one block of 1024 threads, 4096
+   positions per round). */
 static __global__ void __launch_bounds__(1024) KStageList(const int* next, int total, int stage, int* list, int* count)
 {
 	__shared__ int warpSums[32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	int base = 0;
-	for (int k0 = 0; k0 < total; k0 += 1024)
+	for (int k0 = 0; k0 < total; k0 += 4096)
 	{
-		const int k = k0 + threadIdx.x;
-		const bool on = k < total && next[k] == stage;
-		const unsigned m = __ballot_sync(kFull, on);
-		if (lane == 0)
-			warpSums[warp] = __popc(m);
+		const int k = k0 + 4 * int(threadIdx.x);
+		bool on[4];
+		int mine = 0;
+		for (int j = 0; j < 4; j++)
+		{
+			on[j] = k + j < total && next[k + j] == stage;
+			mine += on[j];
+		}
+		/* inclusive scan of the per-thread counts over the warp, then the block */
+		int incl = mine;
+		for (int o = 1; o < 32; o <<= 1)
+		{
+			const int v = __shfl_up_sync(kFull, incl, o);
+			if (lane >= o)
+				incl += v;
+		}
+		if (lane == 31)
+			warpSums[warp] = incl;
 		__syncthreads();
 		int before = 0, all = 0;
 		for (int w = 0; w < 32; w++)
@@ -406,8 +487,10 @@ static __global__ void __launch_bounds__(1024) KStageList(const int* next, int t
 			before += w < warp ? c : 0;
 			all += c;
 		}
-		if (on)
-			list[base + before + __popc(m & ((1u << lane) - 1))] = k;
+		int at = base + before + incl - mine;
+		for (int j = 0; j < 4; j++)
+			if (on[j])
+				list[at++] = k + j;
 		base += all;
 		__syncthreads();
 	}

@@ -22,6 +22,10 @@ cudaError_t LaunchStagedEncode(int grid, cudaStream_t stream, const Job& job, co
 	const LevelTables& T1)
 {
 	cudaError_t e = LaunchStage<kD, kStageDraft>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepDraftRot>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepDraftMode7>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepDraftOpaque31>(grid, stream, job, sg, T0, T1);
+	if (e == cudaSuccess) e = LaunchStage<kD, kStepDraftOpaque20>(grid, stream, job, sg, T0, T1);
 	if (e == cudaSuccess) e = LaunchStage<kD, kStepRefine>(grid, stream, job, sg, T0, T1);
 	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull3Mode2>(grid, stream, job, sg, T0, T1);
 	if (e == cudaSuccess) e = LaunchStage<kD, kStepFull3Mode0>(grid, stream, job, sg, T0, T1);
@@ -45,6 +49,10 @@ template<int kD>
 cudaError_t StagedEncodeOccupancy(int* ctasPerSm)
 {
 	cudaError_t e = PrepareStage<kD, kStageDraft>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepDraftRot>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepDraftMode7>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepDraftOpaque31>();
+	if (e == cudaSuccess) e = PrepareStage<kD, kStepDraftOpaque20>();
 	if (e == cudaSuccess) e = PrepareStage<kD, kStepRefine>();
 	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull3Mode2>();
 	if (e == cudaSuccess) e = PrepareStage<kD, kStepFull3Mode0>();

@@ -8,6 +8,7 @@
 #pragma once
 
 #include "bc7_defs.cuh"
+#include "bc7_encode.cuh"
 
 namespace nebc7 {
 
@@ -176,6 +177,64 @@ __global__ void KBlockBuckets(const uint8_t* bgra, long long stride, int blocksW
 		const unsigned d = __vsubus4(hi, lo);
 		const int range = int(d & 0xFF) + int((d >> 8) & 0xFF) + int((d >> 16) & 0xFF) + int(d >> 24);
 		const int b = 255 - min(255, range >> 2);
+		bucket[k] = uint8_t(b);
+		atomicAdd(&h[b], 1);
+	}
+	__syncthreads();
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		if (h[i])
+			atomicAdd(&hist[i], h[i]);
+}
+
+/* Expected-cost class of a texture's preset (the measured cost ratios
+   draft 1, default 11, precise 400, /slow 480, /data 7200 of a block). */
+__device__ __forceinline__ int CostClass(const TexDesc& d)
+{
+	if (!d.P.doNormal || d.P.doDraft == 2)
+		return 0;
+	if (d.P.wA == 1)
+		return 3;
+	if (d.P.doSlow || d.denoise == 0 || d.P.denoiseStep == 0)
+		return 2;
+	return 1;
+}
+
+/* KBlockBuckets over the queue of a launch of several textures: bucket
+   255 - (64 * cost class + min(63, range / 16)) per queue position, so that
+   the counting sort deals the most expensive preset's widest blocks first. */
+__global__ void KJobBuckets(const TexDesc* tex, int ntex, int total, uint8_t* bucket, int* hist)
+{
+	__shared__ int h[256];
+	for (int i = threadIdx.x; i < 256; i += blockDim.x)
+		h[i] = 0;
+	__syncthreads();
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k < total)
+	{
+		int t = 0, hi = ntex - 1;
+		while (t < hi)
+		{
+			const int mid = (t + hi + 1) >> 1;
+			if (tex[mid].first <= k)
+				t = mid;
+			else
+				hi = mid - 1;
+		}
+		const TexDesc& d = tex[t];
+		const int local = k - d.first;
+		const int bx = local % d.blocksW, by = local / d.blocksW;
+		const uint8_t* p = d.bgra + (long long)by * 4 * d.stride + (long long)bx * 16;
+		unsigned lo = 0xFFFFFFFFu, hv = 0;
+		for (int r = 0; r < 4; r++)
+			for (int x = 0; x < 4; x++)
+			{
+				const unsigned v = *reinterpret_cast<const uint32_t*>(p + r * d.stride + x * 4);
+				lo = __vminu4(lo, v);
+				hv = __vmaxu4(hv, v);
+			}
+		const unsigned dd = __vsubus4(hv, lo);
+		const int range = int(dd & 0xFF) + int((dd >> 8) & 0xFF) + int((dd >> 16) & 0xFF) + int(dd >> 24);
+		const int b = 255 - (64 * CostClass(d) + min(63, range >> 4));
 		bucket[k] = uint8_t(b);
 		atomicAdd(&h[b], 1);
 	}

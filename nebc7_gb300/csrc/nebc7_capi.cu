@@ -36,7 +36,7 @@ struct DeviceTables
 {
 	bool built = false;
 	LevelTables t{};
-	void* mem[14] = {};
+	void* mem[15] = {};
 };
 
 std::mutex gMutex;
@@ -60,13 +60,14 @@ int SetError(int e)
 	} while (0)
 
 /* Bytes of each resident level table, in LevelTables order. */
-constexpr int kNumLevelTables = 14;
+constexpr int kNumLevelTables = 15;
 constexpr size_t kLevelTableBytes[kNumLevelTables] = {
 	size_t(511) * 512, size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 	size_t(256) * 256 * 2, size_t(256) * 64 * 2, size_t(256) * 32 * 2,
 	size_t(256) * 16384, size_t(256) * 4096, size_t(256) * 1024,
 	size_t(256) * 128 * 2, size_t(256) * 32 * 2,
 	size_t(511) * 256, size_t(511) * 256,
+	size_t(511) * 512,
 };
 
 int BuildTables(int dev, int denoise, const LevelTables** out)
@@ -91,7 +92,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 			cudaFree(d3v8);
 			cudaFree(d2v8);
 		};
-		for (int i = 0; i < 14; i++)
+		for (int i = 0; i < kNumLevelTables; i++)
 		{
 			if (cudaMalloc(&D.mem[i], sizes[i]) != cudaSuccess)
 			{
@@ -126,6 +127,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[12], 16, denoise);
 		KBuildHalfDiff<<<grid(511 * 256), tb>>>((uint8_t*)D.mem[13], 4, denoise);
 		KBuildByteDiff<<<grid(511 * 512), tb>>>((uint8_t*)D.mem[0], 4, denoise);
+		KBuildByteDiff<<<grid(511 * 512), tb>>>((uint8_t*)D.mem[14], 8, denoise);
 		const cudaError_t e = cudaDeviceSynchronize();
 		cudaFree(d3v8);
 		cudaFree(d2v8);
@@ -150,6 +152,7 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 		t.c3v5 = (const uint16_t*)D.mem[11];
 		t.d4h = (const uint8_t*)D.mem[12];
 		t.d2h = (const uint8_t*)D.mem[13];
+		t.d3v8 = (const uint8_t*)D.mem[14];
 		D.built = true;
 	}
 	*out = &D.t;
@@ -642,6 +645,13 @@ double BlockCost(const nebc7_settings& s)
 	return 11.0;
 }
 
+/* Block-order scratch of a launch of n blocks: histogram and cursors
+   (2 KB, zeroed per launch), a bucket byte and an order entry per block. */
+size_t OrderScratchBytes(int n)
+{
+	return 2048 + ((size_t(n) + 255) & ~size_t(255)) + ((size_t(n) * 4 + 255) & ~size_t(255));
+}
+
 struct BatchGroup
 {
 	int slot;                 /* kernel instantiation */
@@ -650,6 +660,7 @@ struct BatchGroup
 	int total;                /* blocks */
 	int grid;
 	long long stagedOff;      /* its staged-encode records in the batch's staged area, or -1 */
+	long long orderOff;       /* its block-order scratch in the batch's order area */
 };
 
 struct BatchSchedule
@@ -659,6 +670,7 @@ struct BatchSchedule
 	TexDesc* dTable = nullptr;       /* device copy */
 	cudaGraphExec_t graph = nullptr;
 	size_t stagedBytes = 0;          /* staged-encode records of all its groups */
+	size_t orderBytes = 0;           /* block-order scratch of all its groups */
 };
 
 } // namespace
@@ -673,6 +685,7 @@ struct nebc7_batch
 	int chosen = 0;
 	uint8_t* dmem = nullptr;         /* counters, results, sums */
 	uint8_t* staged = nullptr;       /* per-group records of the staged encodes */
+	uint8_t* orderArea = nullptr;    /* per-group block orders */
 	int* counters = nullptr;
 	BlockResult* results = nullptr;
 	long long* errs = nullptr;
@@ -725,6 +738,7 @@ void BuildSchedule(nebc7_batch* b, int which)
 			g.total = 0;
 			g.grid = 0;
 			g.stagedOff = -1;
+			g.orderOff = 0;
 			S.groups.push_back(g);
 		}
 		BatchGroup& g = S.groups.back();
@@ -747,10 +761,12 @@ void BuildSchedule(nebc7_batch* b, int which)
 		g.total += d.nblocks;
 		queue += d.nblocks;
 	}
-	long long off = 0;
+	long long off = 0, ooff = 0;
 	for (BatchGroup& g : S.groups)
 	{
 		g.grid = GridForSlot(g.total, g.slot);
+		g.orderOff = ooff;
+		ooff += (long long)OrderScratchBytes(g.total);
 		g.stagedOff = -1;
 		if (SlotStaged(g.slot) && g.total > 0)
 		{
@@ -759,6 +775,7 @@ void BuildSchedule(nebc7_batch* b, int which)
 		}
 	}
 	S.stagedBytes = size_t(off);
+	S.orderBytes = size_t(ooff);
 }
 
 /* Enqueues schedule `which` on stream st (capturable): clears the outputs
@@ -793,6 +810,20 @@ int EnqueueSchedule(nebc7_batch* b, int which, cudaStream_t st)
 		job.order = nullptr;
 		job.single = S.table[G.firstTex];
 		const cudaStream_t gs = g == 0 ? st : b->side[g - 1];
+		/* the group's blocks most expensive preset first, widest pixel range
+		   first within a preset (per-texture sums are by block, unchanged) */
+		uint8_t* oa = b->orderArea + G.orderOff;
+		int* hist = (int*)oa;
+		uint8_t* bucket = oa + 2048;
+		int* order = (int*)(bucket + ((size_t(G.total) + 255) & ~size_t(255)));
+		CK(cudaMemsetAsync(hist, 0, 2048, gs));
+		{
+			const int tb = 256, ob = (G.total + tb - 1) / tb;
+			KJobBuckets<<<ob, tb, 0, gs>>>(job.tex, job.ntex, G.total, bucket, hist);
+			KBlockOrder<<<ob, tb, 0, gs>>>(bucket, G.total, hist, hist + 256, order);
+			CK(cudaGetLastError());
+		}
+		job.order = order;
 		CK(LaunchSlot(G.slot, G.grid, gs, job, *b->T[0], *b->T[1], G.stagedOff >= 0 ? b->staged + G.stagedOff : nullptr));
 	}
 	if (ng > 1)
@@ -863,6 +894,7 @@ void FreeBatch(nebc7_batch* b)
 		cudaStreamDestroy(b->cap);
 	cudaFree(b->dmem);
 	cudaFree(b->staged);
+	cudaFree(b->orderArea);
 	delete b;
 }
 
@@ -1620,8 +1652,10 @@ int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_ba
 		const size_t offErr = offRes + ((size_t(total) * sizeof(BlockResult) + 255) & ~size_t(255));
 		const size_t bytes = offErr + size_t(n) * 4 * sizeof(long long);
 		const size_t stagedBytes = std::max(b->sched[0].stagedBytes, b->sched[1].stagedBytes);
+		const size_t orderBytes = std::max(b->sched[0].orderBytes, b->sched[1].orderBytes);
 		if (cudaMalloc((void**)&b->dmem, bytes) != cudaSuccess ||
-			(stagedBytes && cudaMalloc((void**)&b->staged, stagedBytes) != cudaSuccess))
+			(stagedBytes && cudaMalloc((void**)&b->staged, stagedBytes) != cudaSuccess) ||
+			cudaMalloc((void**)&b->orderArea, orderBytes) != cudaSuccess)
 			rc = SetError(NEBC7_ENOMEM);
 		else
 		{

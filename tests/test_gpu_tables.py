@@ -62,10 +62,32 @@ def test_device_table_equals_port(native, port, denoise, name):
         assert np.array_equal(got.reshape(-1), ref[x]), f"{name} x={x}"
 
 
+def _expanded(bits):
+    q = np.arange(1 << bits)
+    return (q << (8 - bits)) | (q >> (2 * bits - 8)) if bits < 8 else q
+
+
+@pytest.mark.parametrize("denoise", [0, 1])
+@pytest.mark.parametrize("name,diff_index,bits", [("d2v7", 0, 7), ("d2v6", 0, 6), ("d2v5", 0, 5), ("d3v6", 14, 6),
+                                                   ("d3v5", 14, 5)])
+def test_reduced_tables_read_by_differences(native, port, denoise, name, diff_index, bits):
+    """The encoder reads each reduced table of 2- or 3-bit indices as the
+    device's difference table of that index width at the bit-replicated
+    endpoints (d2v8, and d3v8 for 3-bit indices): every x, cL, cH gives the
+    port's entry."""
+    diff = _device_table(native, denoise, diff_index).reshape(511, 512)
+    ref = _port_table(port, denoise, NAMES.index(name)).reshape(256, -1)
+    e = _expanded(bits)
+    eH, eL = np.meshgrid(e, e, indexing="ij")
+    for x in range(256):
+        got = diff[eH - x + 255, eL - x + 255].reshape(-1)
+        assert np.array_equal(got, ref[x]), f"{name} x={x}"
+
+
 def test_table_read_rejects_bad_arguments(native):
     n = ctypes.c_longlong()
     small = np.zeros(16, np.uint8)
-    assert native.nebc7_table_read(1, 14, small.ctypes.data, small.nbytes, ctypes.byref(n)) == 1
+    assert native.nebc7_table_read(1, 15, small.ctypes.data, small.nbytes, ctypes.byref(n)) == 1
     assert native.nebc7_table_read(2, 0, small.ctypes.data, small.nbytes, ctypes.byref(n)) == 1
     assert native.nebc7_table_read(1, 0, small.ctypes.data, small.nbytes, ctypes.byref(n)) == 6
     assert n.value == 511 * 512
