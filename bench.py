@@ -417,8 +417,8 @@ def run_ours(args, rank, world, local):
     px = pw * ph
     value = px * world / (step_ms / 1e3) / 1e6
     # kernels of this library per encode call: the refining variants order the
-    # blocks first (bucket and scatter kernels), then KEncode
-    launches_per_encode = 3 if (st.doNormal and st.doDraft != 2) else 1
+    # blocks first (bucket and scatter kernels), then KEncode or its staged form
+    launches_per_encode = lib.nebc7_encode_launches(ctypes.byref(st))
 
     # end to end through the C ABI host entry (pinned host buffers, copies inside)
     h_img = torch.from_numpy(padded).pin_memory()
@@ -569,6 +569,7 @@ def run_batch(args, rank, world, local):
                for t in texs], from_scratch=True)
     tune_ms = b.tune(1)
     info = b.info()
+    plan, trials = b.plan(), b.trials()
     for _ in range(args.warmup):
         b.launch(sp)
     torch.cuda.synchronize()
@@ -631,6 +632,7 @@ def run_batch(args, rank, world, local):
                        "draft / default / precise", "l2": "inputs (%.0f MB) larger than L2" % (h2d / 1e6),
                        "bit_exact_vs_plain_launches": bool(exact), "schedule": info["schedule"],
                        "launches_per_step": info["launches"], "tune_ms": list(tune_ms),
+                       "plan": plan, "tuner_trials": trials,
                        "parallelism": f"replicas{world}"},
             "plain_per_image": {"value": px / (plain_ms / 1e3) / 1e6, "unit": "Mpx/s", "ms": plain_ms,
                                 "launches": len(texs)},

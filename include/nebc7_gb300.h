@@ -143,6 +143,13 @@ int nebc7_decode_device(const uint8_t* d_blocks, uint8_t* d_bgra, long long stri
 /* Decodes n blocks to 64 bytes of BGRA each (host buffers). */
 int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
 
+/* How many kernels one nebc7_encode_device call with these settings
+   launches (the block order, then the encode: one persistent kernel, or
+   for the presets whose time goes to the full searches the staged form of
+   a kernel per pass and a list kernel before each), not counting the sums'
+   reduction; a negative error code for invalid settings. */
+int nebc7_encode_launches(const nebc7_settings* settings);
+
 /* Builds the level tables of `denoise` on the current device ahead of use. */
 int nebc7_init_device(int denoise);
 
@@ -211,10 +218,11 @@ typedef struct nebc7_batch nebc7_batch;
    stay the caller's and must outlive the plan. */
 int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_batch** out);
 
-/* Times both schedules `trials` times (as CUDA graphs) and keeps the faster
-   for nebc7_batch_launch; restores the starting blocks afterwards unless
-   the plan clears them itself.  ms_out[2], if non-null, receives the best
-   times of the mixed and the grouped schedule (3.4e38 if not tried). */
+/* Tunes the plan (nebc7_batch_trials lists the search): each candidate is
+   replayed `trials` times as a CUDA graph and the fastest is kept for
+   nebc7_batch_launch; restores the starting blocks afterwards unless the
+   plan clears them itself.  ms_out[2], if non-null, receives the best times
+   of the mixed and the grouped schedule (3.4e38 if not tried). */
 int nebc7_batch_tune(nebc7_batch* b, int trials, float* ms_out);
 
 /* Enqueues the batch on `stream` by replaying its CUDA graph (captured on
@@ -229,6 +237,21 @@ int nebc7_batch_sums(nebc7_batch* b, void* stream, int64_t* errs, double* ssim);
 
 /* Overrides the schedule: 0 one mixed launch, 1 one launch per preset group. */
 int nebc7_batch_set_schedule(nebc7_batch* b, int schedule);
+
+/* The plan's knobs: the schedule (0 mixed, 1 grouped), whether the groups
+   whose presets run the full searches use the staged form (one kernel per
+   pass; 1) or one kernel (0), and the resident CTAs per SM of the
+   persistent launches (0: as many as fit).  nebc7_batch_set_plan drops the
+   captured graphs when the staged form or the CTAs change. */
+int nebc7_batch_plan(const nebc7_batch* b, int* schedule, int* staged, int* ctas_per_sm);
+int nebc7_batch_set_plan(nebc7_batch* b, int schedule, int staged, int ctas_per_sm);
+
+/* The plans the last nebc7_batch_tune timed, in order, with their best ms
+   (arrays of cap entries, any may be null); returns how many there were.
+   The tuner starts from one mixed launch, staged, at full occupancy, and
+   keeps each change that is faster: the grouped schedule, then one kernel
+   per group, then 2 CTAs per SM. */
+int nebc7_batch_trials(const nebc7_batch* b, int* schedule, int* staged, int* ctas_per_sm, float* ms, int cap);
 
 /* Chosen schedule (0 mixed, 1 grouped), kernel launches per run, blocks. */
 int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* blocks);

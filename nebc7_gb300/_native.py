@@ -161,6 +161,7 @@ SIGNATURES = {
     "nebc7_decode_device": (I, [VP, VP, LL, I, I, VP]),
     "nebc7_decode_blocks_host": (I, [VP, VP, I]),
     "nebc7_init_device": (I, [I]),
+    "nebc7_encode_launches": (I, [ctypes.POINTER(Settings)]),
     "nebc7_table_read": (I, [I, I, VP, LL, ctypes.POINTER(LL)]),
     "nebc7_launch_shape": (I, [VP, VP, VP]),
     "nebc7_encode_device_noalloc": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),
@@ -170,6 +171,9 @@ SIGNATURES = {
     "nebc7_batch_sums": (I, [VP, VP, VP, VP]),
     "nebc7_batch_set_schedule": (I, [VP, I]),
     "nebc7_batch_info": (I, [VP, VP, VP, VP]),
+    "nebc7_batch_plan": (I, [VP, VP, VP, VP]),
+    "nebc7_batch_set_plan": (I, [VP, I, I, I]),
+    "nebc7_batch_trials": (I, [VP, VP, VP, VP, VP, I]),
     "nebc7_batch_destroy": (None, [VP]),
     "nebc7_server_create": (I, [VP, VP]),
     "nebc7_server_submit": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),

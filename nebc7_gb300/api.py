@@ -289,6 +289,26 @@ class Batch:
     def set_schedule(self, which: int) -> None:
         check(self._lib.nebc7_batch_set_schedule(self._h, which), "batch_set_schedule")
 
+    def plan(self) -> dict:
+        """The plan's knobs: schedule, staged form, CTAs per SM (0: occupancy)."""
+        s, st, c = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.nebc7_batch_plan(self._h, ctypes.byref(s), ctypes.byref(st), ctypes.byref(c)), "batch_plan")
+        return {"schedule": ("mixed", "grouped")[s.value], "staged": bool(st.value), "ctas_per_sm": c.value}
+
+    def set_plan(self, schedule: int, staged: bool, ctas_per_sm: int = 0) -> None:
+        check(self._lib.nebc7_batch_set_plan(self._h, schedule, int(staged), ctas_per_sm), "batch_set_plan")
+
+    def trials(self) -> list[dict]:
+        """The plans the last tune timed, in order, with their best ms."""
+        n = self._lib.nebc7_batch_trials(self._h, None, None, None, None, 0)
+        if n <= 0:
+            return []
+        s, st, c = (ctypes.c_int * n)(), (ctypes.c_int * n)(), (ctypes.c_int * n)()
+        ms = (ctypes.c_float * n)()
+        self._lib.nebc7_batch_trials(self._h, s, st, c, ms, n)
+        return [{"schedule": ("mixed", "grouped")[s[i]], "staged": bool(st[i]), "ctas_per_sm": c[i],
+                 "ms": float(ms[i])} for i in range(n)]
+
     def launch(self, stream: int = 0) -> None:
         check(self._lib.nebc7_batch_launch(self._h, stream), "batch_launch")
 

@@ -248,7 +248,17 @@ struct LaunchShape
 std::mutex gShapeMutex;
 LaunchShape gShapes[kMaxDevices];
 
+/* Grid of a persistent launch of `slot` over nblocks blocks: one CTA per
+   kWarpsPerCta blocks up to the resident CTAs of every SM, or up to
+   ctasPerSm per SM when that is given (> 0) and smaller. */
+int GridForSlotCap(int nblocks, int slot, int ctasPerSm);
+
 int GridForSlot(int nblocks, int slot)
+{
+	return GridForSlotCap(nblocks, slot, 0);
+}
+
+int GridForSlotCap(int nblocks, int slot, int ctasPerSm)
 {
 	int dev = 0;
 	if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
@@ -281,6 +291,8 @@ int GridForSlot(int nblocks, int slot)
 		sms = L.sms;
 		perSm = L.perSm[slot];
 	}
+	if (ctasPerSm > 0 && ctasPerSm < perSm)
+		perSm = ctasPerSm;
 	const int ctasNeeded = (nblocks + kWarpsPerCta - 1) / kWarpsPerCta;
 	const int g = sms * perSm;
 	return ctasNeeded < g ? ctasNeeded : g;
@@ -684,7 +696,7 @@ struct nebc7_batch
 	BatchSchedule sched[2];          /* 0: one mixed launch; 1: one launch per preset group */
 	int chosen = 0;
 	uint8_t* dmem = nullptr;         /* counters, results, sums */
-	uint8_t* staged = nullptr;       /* per-group records of the staged encodes */
+	uint8_t* stagedArea = nullptr;   /* per-group records of the staged encodes */
 	uint8_t* orderArea = nullptr;    /* per-group block orders */
 	int* counters = nullptr;
 	BlockResult* results = nullptr;
@@ -694,6 +706,16 @@ struct nebc7_batch
 	std::vector<cudaStream_t> side;  /* concurrent preset groups */
 	std::vector<cudaEvent_t> ev;     /* fork / join */
 	const LevelTables* T[2] = { nullptr, nullptr };
+	/* the plan's knobs besides the schedule: the staged form of the groups
+	   that have one, and the resident CTAs per SM (0: the occupancy) */
+	int staged = 1;
+	int ctasPerSm = 0;
+	struct Trial
+	{
+		int schedule, staged, ctasPerSm;
+		float ms;
+	};
+	std::vector<Trial> trials;   /* the last tuning's measurements */
 };
 
 namespace {
@@ -764,7 +786,7 @@ void BuildSchedule(nebc7_batch* b, int which)
 	long long off = 0, ooff = 0;
 	for (BatchGroup& g : S.groups)
 	{
-		g.grid = GridForSlot(g.total, g.slot);
+		g.grid = GridForSlotCap(g.total, g.slot, b->ctasPerSm);
 		g.orderOff = ooff;
 		ooff += (long long)OrderScratchBytes(g.total);
 		g.stagedOff = -1;
@@ -824,7 +846,8 @@ int EnqueueSchedule(nebc7_batch* b, int which, cudaStream_t st)
 			CK(cudaGetLastError());
 		}
 		job.order = order;
-		CK(LaunchSlot(G.slot, G.grid, gs, job, *b->T[0], *b->T[1], G.stagedOff >= 0 ? b->staged + G.stagedOff : nullptr));
+		CK(LaunchSlot(G.slot, G.grid, gs, job, *b->T[0], *b->T[1],
+			(b->staged && G.stagedOff >= 0) ? b->stagedArea + G.stagedOff : nullptr));
 	}
 	if (ng > 1)
 	{
@@ -875,6 +898,31 @@ int GraphFor(nebc7_batch* b, int which, cudaGraphExec_t* out)
 	return NEBC7_OK;
 }
 
+/* Sets the plan's knobs; a change of the staged form or of the grid drops
+   the captured graphs, which the next launch captures again. */
+int ApplyPlan(nebc7_batch* b, int schedule, int staged, int ctasPerSm)
+{
+	if (staged != b->staged || ctasPerSm != b->ctasPerSm)
+	{
+		b->staged = staged;
+		b->ctasPerSm = ctasPerSm;
+		for (BatchSchedule& S : b->sched)
+		{
+			if (S.graph)
+				cudaGraphExecDestroy(S.graph);
+			S.graph = nullptr;
+			for (BatchGroup& g : S.groups)
+			{
+				g.grid = GridForSlotCap(g.total, g.slot, ctasPerSm);
+				if (g.grid <= 0 && g.total > 0)
+					return SetError(NEBC7_ECUDA);
+			}
+		}
+	}
+	b->chosen = schedule;
+	return NEBC7_OK;
+}
+
 void FreeBatch(nebc7_batch* b)
 {
 	if (!b)
@@ -893,7 +941,7 @@ void FreeBatch(nebc7_batch* b)
 	if (b->cap)
 		cudaStreamDestroy(b->cap);
 	cudaFree(b->dmem);
-	cudaFree(b->staged);
+	cudaFree(b->stagedArea);
 	cudaFree(b->orderArea);
 	delete b;
 }
@@ -1588,6 +1636,14 @@ int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n)
 	return rc;
 }
 
+int nebc7_encode_launches(const nebc7_settings* settings)
+{
+	if (int e = ValidateSettings(settings))
+		return -SetError(e);
+	const int order = OrdersBlocks(*settings) ? 2 : 0;
+	return order + (SlotStaged(VariantSlot(*settings)) ? 1 + 2 * kNumStages : 1);
+}
+
 int nebc7_init_device(int denoise)
 {
 	if (denoise != 0 && denoise != 1)
@@ -1654,7 +1710,7 @@ int nebc7_batch_create(const nebc7_texture* textures, int n, int flags, nebc7_ba
 		const size_t stagedBytes = std::max(b->sched[0].stagedBytes, b->sched[1].stagedBytes);
 		const size_t orderBytes = std::max(b->sched[0].orderBytes, b->sched[1].orderBytes);
 		if (cudaMalloc((void**)&b->dmem, bytes) != cudaSuccess ||
-			(stagedBytes && cudaMalloc((void**)&b->staged, stagedBytes) != cudaSuccess) ||
+			(stagedBytes && cudaMalloc((void**)&b->stagedArea, stagedBytes) != cudaSuccess) ||
 			cudaMalloc((void**)&b->orderArea, orderBytes) != cudaSuccess)
 			rc = SetError(NEBC7_ENOMEM);
 		else
@@ -1740,31 +1796,62 @@ int nebc7_batch_tune(nebc7_batch* b, int trials, float* ms_out)
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
 	if (rc == NEBC7_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
 		rc = SetError(NEBC7_ECUDA);
-	for (int trial = 0; trial < trials && rc == NEBC7_OK; trial++)
-	{
-		for (int w = 0; w < 2 && rc == NEBC7_OK; w++)
+	/* best of `trials` replays of one plan's graph */
+	auto measure = [&](int schedule, int staged, int ctas, float* out) -> int {
+		if (int e = ApplyPlan(b, schedule, staged, ctas))
+			return e;
+		float m = 3.4e38f;
+		for (int trial = 0; trial < trials; trial++)
 		{
-			if (w == 1 && b->sched[1].groups.size() < 2)
-				continue;   /* same as the mixed launch */
 			cudaGraphExec_t g = nullptr;
-			rc = GraphFor(b, w, &g);
-			if (rc != NEBC7_OK)
-				break;
+			if (int e = GraphFor(b, schedule, &g))
+				return e;
 			restore();
 			if (cudaEventRecord(e0, b->cap) != cudaSuccess || cudaGraphLaunch(g, b->cap) != cudaSuccess ||
 				cudaEventRecord(e1, b->cap) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
-			{
-				rc = SetError(NEBC7_ECUDA);
-				break;
-			}
+				return SetError(NEBC7_ECUDA);
 			float ms = 0;
 			cudaEventElapsedTime(&ms, e0, e1);
-			best[w] = std::min(best[w], ms);
+			m = std::min(m, ms);
 		}
-	}
+		b->trials.push_back(nebc7_batch::Trial{ schedule, staged, ctas, m });
+		best[schedule] = std::min(best[schedule], m);
+		*out = m;
+		return NEBC7_OK;
+	};
+	/* coordinate search from one mixed launch in the staged form at full
+	   occupancy: the schedule, then the staged form, then fewer CTAs per SM,
+	   each kept when it is faster */
+	b->trials.clear();
+	bool anyStaged = false;
+	for (const BatchSchedule& S : b->sched)
+		for (const BatchGroup& g : S.groups)
+			anyStaged |= g.stagedOff >= 0;
+	int cur[3] = { 0, 1, 0 };
+	float curMs = 0;
+	if (rc == NEBC7_OK)
+		rc = measure(cur[0], cur[1], cur[2], &curMs);
+	auto tryPlan = [&](int schedule, int staged, int ctas) {
+		if (rc != NEBC7_OK)
+			return;
+		float m = 0;
+		rc = measure(schedule, staged, ctas, &m);
+		if (rc == NEBC7_OK && m < curMs)
+		{
+			cur[0] = schedule;
+			cur[1] = staged;
+			cur[2] = ctas;
+			curMs = m;
+		}
+	};
+	if (b->sched[1].groups.size() >= 2)
+		tryPlan(1, cur[1], cur[2]);
+	if (anyStaged)
+		tryPlan(cur[0], 0, cur[2]);
+	tryPlan(cur[0], cur[1], 2);
 	if (rc == NEBC7_OK)
 	{
-		b->chosen = best[1] < best[0] ? 1 : 0;
+		rc = ApplyPlan(b, cur[0], cur[1], cur[2]);
 		if (ms_out)
 		{
 			ms_out[0] = best[0];
@@ -1815,6 +1902,47 @@ int nebc7_batch_set_schedule(nebc7_batch* b, int schedule)
 	return NEBC7_OK;
 }
 
+int nebc7_batch_plan(const nebc7_batch* b, int* schedule, int* staged, int* ctas_per_sm)
+{
+	if (!b)
+		return SetError(NEBC7_EINVAL);
+	if (schedule)
+		*schedule = b->chosen;
+	if (staged)
+		*staged = b->staged;
+	if (ctas_per_sm)
+		*ctas_per_sm = b->ctasPerSm;
+	return NEBC7_OK;
+}
+
+int nebc7_batch_set_plan(nebc7_batch* b, int schedule, int staged, int ctas_per_sm)
+{
+	if (!b || schedule < 0 || schedule > 1 || staged < 0 || staged > 1 || ctas_per_sm < 0 || ctas_per_sm > 64)
+		return SetError(NEBC7_EINVAL);
+	CK(cudaSetDevice(b->device));
+	return ApplyPlan(b, schedule, staged, ctas_per_sm);
+}
+
+int nebc7_batch_trials(const nebc7_batch* b, int* schedule, int* staged, int* ctas_per_sm, float* ms, int cap)
+{
+	if (!b || cap < 0)
+		return SetError(NEBC7_EINVAL);
+	const int n = int(b->trials.size());
+	for (int i = 0; i < n && i < cap; i++)
+	{
+		const nebc7_batch::Trial& t = b->trials[i];
+		if (schedule)
+			schedule[i] = t.schedule;
+		if (staged)
+			staged[i] = t.staged;
+		if (ctas_per_sm)
+			ctas_per_sm[i] = t.ctasPerSm;
+		if (ms)
+			ms[i] = t.ms;
+	}
+	return n;
+}
+
 int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* blocks)
 {
 	if (!b)
@@ -1822,7 +1950,14 @@ int nebc7_batch_info(const nebc7_batch* b, int* schedule, int* launches, int* bl
 	if (schedule)
 		*schedule = b->chosen;
 	if (launches)
-		*launches = int(b->sched[b->chosen].groups.size());
+	{
+		/* per group: the block order (2), the encode (the staged form: the
+		   first kernel, then a list and a kernel per stage), the sums */
+		int n = 0;
+		for (const BatchGroup& g : b->sched[b->chosen].groups)
+			n += 2 + ((b->staged && g.stagedOff >= 0) ? 1 + 2 * kNumStages : 1) + 1;
+		*launches = n;
+	}
 	if (blocks)
 		*blocks = b->totalBlocks;
 	return NEBC7_OK;

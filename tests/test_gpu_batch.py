@@ -70,6 +70,26 @@ def test_batch_matches_plain_launches(native, schedule):
     b.close()
 
 
+@pytest.mark.parametrize("plan", [(0, 0, 0), (0, 1, 1), (1, 0, 2), (1, 1, 3)])
+def test_every_plan_gives_the_plain_blocks(native, plan):
+    """The tuner's knobs (schedule, staged form, CTAs per SM) change how the
+    blocks are scheduled, never what they are."""
+    torch = pytest.importorskip("torch")
+    texs = _textures(torch, 15, 53, 4, 96, ["precise", "default", "slow", "draft", "data"])
+    want = [_plain(native, torch, t) for t in texs]
+    b = _batch(texs)
+    b.set_plan(*plan)
+    assert b.plan() == {"schedule": ("mixed", "grouped")[plan[0]], "staged": bool(plan[1]), "ctas_per_sm": plan[2]}
+    b.launch()
+    errs, ssim = b.sums()
+    for i, t in enumerate(texs):
+        blocks, e, q = want[i]
+        assert np.array_equal(t["dst"].cpu().numpy(), blocks), f"texture {i} ({t['preset']})"
+        assert errs[i].tolist() == e.tolist()
+        assert np.array_equal(ssim[i], q)
+    b.close()
+
+
 def test_batch_tune_keeps_outputs_and_starting_blocks(native):
     torch = pytest.importorskip("torch")
     texs = _textures(torch, 12, 47, 16, 256)
@@ -87,6 +107,12 @@ def test_batch_tune_keeps_outputs_and_starting_blocks(native):
         assert errs[i].tolist() == want[i][1].tolist()
     info = b.info()
     assert info["blocks"] == sum((t["w"] // 4) * (t["h"] // 4) for t in texs)
+    trials = b.trials()
+    assert len(trials) >= 2 and all(t["ms"] > 0 for t in trials)
+    p = b.plan()
+    assert min(t["ms"] for t in trials) == min(t["ms"] for t in trials
+                                               if (t["schedule"], t["staged"], t["ctas_per_sm"]) ==
+                                               (p["schedule"], p["staged"], p["ctas_per_sm"]))
     b.close()
 
 
