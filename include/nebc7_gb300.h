@@ -294,12 +294,16 @@ typedef struct nebc7_server_counters
    hbm_budget bytes holds the sources, masks, outputs and per-block results
    of the requests in flight.  A scheduler thread admits requests in
    arrival order while the arena has room, and starts a batch of admitted
-   requests (one persistent launch over their blocks, presets mixed) on
-   every free stream, so requests that arrive while others run join the
-   device as soon as a stream and memory free up.  Within a launch the
-   cheapest requests are dealt first, and each request returns (its blocks
-   copied back) as soon as its own blocks are done, while the rest of the
-   launch still runs. */
+   requests on every free stream, so requests that arrive while others run
+   join the device as soon as a stream and memory free up.  A batch is the
+   oldest admitted request and later ones of its kind: heavy presets (the
+   precise preset, /slow, /data) run as one staged launch (a kernel per
+   pass), light ones as one persistent launch with presets mixed, the
+   cheapest requests dealt first; each request of a light batch returns
+   (its blocks copied back) as soon as its own blocks are done, while the
+   rest of the launch still runs.  Besides the arena, every stream holds the
+   staged form's records: 104 bytes per block for up to min(4194304,
+   hbm_budget / 104) blocks. */
 int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out);
 
 /* Queues one texture (host buffers; pinned memory lets the copies run

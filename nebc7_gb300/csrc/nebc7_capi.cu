@@ -993,6 +993,8 @@ struct ServerSlot
 	long long* hSums = nullptr;      /* pinned: 2 errs + 2 ssim (as bits) per request */
 	long long* dSums = nullptr;
 	int* dCounter = nullptr;
+	uint8_t* staged = nullptr;       /* records of a staged launch of up to stagedCap blocks */
+	int stagedCap = 0;
 };
 
 /* First-fit allocator over the arena (offsets, host bookkeeping only). */
@@ -1068,6 +1070,18 @@ struct nebc7_server
 
 namespace {
 
+/* Arena bytes a block needs at least (its pixels, output and result), and
+   the most blocks one staged launch of the request loop holds records for. */
+constexpr size_t kServerBlockBytes = 64 + 16 + sizeof(BlockResult);
+constexpr int kServerStagedBlocks = 1 << 22;
+
+/* A request whose preset runs the full searches on most blocks (the
+   precise preset, /slow, /data). */
+bool HeavyRequest(const ServerRequest& r)
+{
+	return BlockCost(r.settings) >= 400.0;
+}
+
 size_t RequestBytes(const ServerRequest& r)
 {
 	const size_t nb = size_t(r.w / 4) * (r.h / 4);
@@ -1136,7 +1150,13 @@ int LaunchServerBatch(nebc7_server* sv, ServerSlot& slot, std::vector<int64_t>& 
 	const int grid = GridForSlot(total, kVariantMixed);
 	if (grid <= 0)
 		return SetError(NEBC7_ECUDA);
-	CK(kVariants[kVariantMixed].launch(grid, st, job, *sv->T[0], *sv->T[1]));
+	/* a batch of heavy requests takes the staged form (one kernel per pass);
+	   a batch of light ones the single kernel, whose blocks and so whose
+	   requests finish as they go */
+	bool heavy = total <= slot.stagedCap;
+	for (int64_t id : batch)
+		heavy = heavy && HeavyRequest(sv->reqs[id]);
+	CK(LaunchSlot(kVariantMixed, grid, st, job, *sv->T[0], *sv->T[1], heavy ? slot.staged : nullptr));
 	CK(cudaEventRecord(slot.done, st));
 	slot.stage.assign(batch.size(), 0);
 	return NEBC7_OK;
@@ -1264,11 +1284,24 @@ void ServerLoop(nebc7_server* sv)
 		{
 			if (slot.busy || sv->admitted.empty())
 				continue;
+			/* the oldest admitted request and, in arrival order, others of its
+			   kind (heavy or light presets) up to max_batch requests and, for
+			   heavy ones, the staged records' capacity */
 			std::vector<int64_t> batch;
-			while (!sv->admitted.empty() && int(batch.size()) < sv->cfg.max_batch)
+			const bool heavy = HeavyRequest(sv->reqs[sv->admitted.front()]);
+			long long blocks = 0;
+			for (auto it = sv->admitted.begin(); it != sv->admitted.end() && int(batch.size()) < sv->cfg.max_batch;)
 			{
-				batch.push_back(sv->admitted.front());
-				sv->admitted.pop_front();
+				const ServerRequest& r = sv->reqs[*it];
+				const long long nb = (long long)(r.w / 4) * (r.h / 4);
+				if (HeavyRequest(r) != heavy || (!batch.empty() && heavy && blocks + nb > slot.stagedCap))
+				{
+					++it;
+					continue;
+				}
+				blocks += nb;
+				batch.push_back(*it);
+				it = sv->admitted.erase(it);
 			}
 			const double now = NowSeconds();
 			for (int64_t id : batch)
@@ -1342,6 +1375,7 @@ void FreeServer(nebc7_server* sv)
 		cudaFree(slot.dTable);
 		cudaFree(slot.dSums);
 		cudaFree(slot.dCounter);
+		cudaFree(slot.staged);
 	}
 	cudaFree(sv->arena);
 	delete sv;
@@ -2010,6 +2044,11 @@ int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out)
 			cudaMalloc((void**)&slot.dTable, sizeof(TexDesc) * cap) != cudaSuccess ||
 			cudaMalloc((void**)&slot.dSums, sizeof(long long) * 4 * cap) != cudaSuccess ||
 			cudaMalloc((void**)&slot.dCounter, 256) != cudaSuccess)
+			rc = SetError(NEBC7_ENOMEM);
+		/* the staged form's records: a launch holds at most one block per
+		   kServerBlockBytes of the arena */
+		slot.stagedCap = int(std::min<size_t>(kServerStagedBlocks, cfg->hbm_budget / kServerBlockBytes + 1));
+		if (rc == NEBC7_OK && cudaMalloc((void**)&slot.staged, StagedScratchBytes(slot.stagedCap)) != cudaSuccess)
 			rc = SetError(NEBC7_ENOMEM);
 	}
 	/* size the mixed kernel's launch before any request arrives */
