@@ -24,6 +24,16 @@
 namespace nebc7 {
 
 constexpr bool kHasNormalPasses = true;
+
+/* Whether the scans read the reduced tables of 2- and 3-bit indices through
+   the 8-bit difference tables (DiffBase) or in the reference's per-x
+   layout.  The difference tables serve the full searches best; the compact
+   default-preset kernel, whose time goes to the Mode6Index2 refinement,
+   keeps the per-x layout (its translation unit sets 0). */
+#ifndef NEBC7_REDUCED_BY_DIFF
+#define NEBC7_REDUCED_BY_DIFF 1
+#endif
+constexpr bool kReducedByDiff = NEBC7_REDUCED_BY_DIFF != 0;
 constexpr int kBig = 0x7FFFFFFF;
 
 struct __align__(16) SearchState
@@ -285,11 +295,11 @@ __device__ __forceinline__ Spec3 GetSpec3(const LevelTables& T)
 	/* mode 1's shared p-bit table marks endpoint pairs of different parity
 	   (0xFF), which its estimates read: it stays in the per-x layout */
 	if (MODE == 0)
-		return Spec3{ 4, T.d3v8, true, 5, T.c3v5 };
+		return Spec3{ 4, kReducedByDiff ? T.d3v8 : T.d3v5, kReducedByDiff, 5, T.c3v5 };
 	if (MODE == 1)
 		return Spec3{ 6, T.d3v7s, false, 7, T.c3v7s };
 	if (MODE == 2)
-		return Spec3{ 5, T.d2v8, true, 5, T.c2v5 };
+		return Spec3{ 5, kReducedByDiff ? T.d2v8 : T.d2v5, kReducedByDiff, 5, T.c2v5 };
 	return Spec3{ 7, T.d2v8, true, 8, T.c2v8 };
 }
 
@@ -755,7 +765,8 @@ __device__ NEBC7_PASS bool InitLevels4(SearchState& ss, int v, int pbits, const 
 		}
 		else
 		{
-			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, T.d2v8, true, 20,
+			cl[c] = ChannelLevels<kD, false>(ss.lists[v][c], ar, ai, c, wts[c], water - used - rest, 5, pbits, c != 0, kReducedByDiff ? T.d2v8 : T.d2v6,
+				kReducedByDiff, 20,
 				ss.uniq, lane);
 		}
 		used += cl[c].minErr;
@@ -895,7 +906,8 @@ __device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const
 		}
 		if (!ai.opaque)
 		{
-			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, T.d2v8, true, T.c2v6, ss.uniq, lane);
+			const int l0 = EstimateChannelLevels<kD>(ar, ai, 0, P.wA, water - error, 6, false, kReducedByDiff ? T.d2v8 : T.d2v6, kReducedByDiff,
+				T.c2v6, ss.uniq, lane);
 			est[0] = l0;
 			error += l0;
 		}
@@ -906,7 +918,8 @@ __device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const
 		{
 			if (!(error < water))
 				return water;
-			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, T.d2v8, true, T.c2v6, ss.uniq, lane);
+			const int l = EstimateChannelLevels<kD>(ar, ai, c, wts[c], water - error, 6, true, kReducedByDiff ? T.d2v8 : T.d2v6, kReducedByDiff,
+				T.c2v6, ss.uniq, lane);
 			est[c] = l;
 			error += l;
 		}
@@ -1083,14 +1096,14 @@ __device__ NEBC7_PASS int CompressRotSubset(WarpState& st, SearchState& ss, cons
 	{
 		cbits = 5;
 		abits = 6;
-		ctab = idx32 ? T.d3v8 : T.d2v8;
-		atab = idx32 ? T.d2v8 : T.d3v8;
+		ctab = kReducedByDiff ? (idx32 ? T.d3v8 : T.d2v8) : (idx32 ? T.d3v5 : T.d2v5);
+		atab = kReducedByDiff ? (idx32 ? T.d2v8 : T.d3v8) : (idx32 ? T.d2v6 : T.d3v6);
 	}
 	else
 	{
 		cbits = 7;
 		abits = 8;
-		ctab = T.d2v8;
+		ctab = kReducedByDiff ? T.d2v8 : T.d2v7;
 		atab = T.d2v8;
 	}
 	const int wts[4] = { P.wA, P.wG, P.wR, P.wB };
@@ -1101,9 +1114,11 @@ __device__ NEBC7_PASS int CompressRotSubset(WarpState& st, SearchState& ss, cons
 		if (c == 0 && ai.opaque)
 			cl[0] = ZeroList(ss.lists[0][0], 0xFFFF, lane);
 		else if (c == a)
-			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, true, ss.uniq, lane);
+			cl[c] = ChannelLevelsSingle<kD>(ss.lists[0][c], ar, ai, c, wts[c], water - used, abits, c != 0, atab, kReducedByDiff || abits == 8,
+				ss.uniq, lane);
 		else
-			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, true, 32, ss.uniq, lane);
+			cl[c] = ChannelLevels<kD, false>(ss.lists[0][c], ar, ai, c, wts[c], water - used, cbits, -1, c != 0, ctab, kReducedByDiff, 32,
+				ss.uniq, lane);
 		used += cl[c].minErr;
 		if (used >= water)
 			return water;
