@@ -37,6 +37,16 @@ __device__ __forceinline__ int Wadd(int a, int b) { return int(unsigned(a) + uns
 __device__ __forceinline__ int Wsub(int a, int b) { return int(unsigned(a) - unsigned(b)); }
 __device__ __forceinline__ unsigned Shr32(unsigned v, unsigned s) { return v >> (s & 31); }
 
+/* Whether the scans read the reduced tables of 2- and 3-bit indices through
+   the 8-bit difference tables (DiffBase) or in the reference's per-x
+   layout.  The difference tables serve the full searches best; the compact
+   default-preset kernel, whose time goes to the Mode6Index2 refinement,
+   keeps the per-x layout (its translation unit sets 0). */
+#ifndef NEBC7_REDUCED_BY_DIFF
+#define NEBC7_REDUCED_BY_DIFF 1
+#endif
+constexpr bool kReducedByDiff = NEBC7_REDUCED_BY_DIFF != 0;
+
 /* A reduced table's s-bit endpoint expanded to 8 bits by bit replication. */
 __device__ __forceinline__ int ExpandTo8(int v, int s)
 {
@@ -224,7 +234,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 	/* byte tables by (x, c); with 8-bit endpoints (shift 8) the byte table
 	   goes by DiffAt and the half tables by HalfAt */
 	const int rowSize = 1 << (2 * shift);
-	const bool diff = shift == 8 || byDiff;
+	const bool diff = shift == 8 || (kReducedByDiff && byDiff);
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 	const bool pvar = HALF || pbits >= 0;
 	const int pH = reverse ? (pbits & 1) : (pbits >> 8);
@@ -274,7 +284,8 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 			unsigned key = 0xFFFFFFFFu;
 			if (on)
 			{
-				const int dbase = DiffBase(cc, shift);
+				/* the per-x build reads the 8-bit table by DiffAt, as DiffBase with s = 8 */
+				const int dbase = kReducedByDiff ? DiffBase(cc, shift) : 0;
 				/* four distinct values per step, their table reads in flight
 				   together (unsigned sums do not depend on the order) */
 				auto term = [&](int e) {
@@ -283,7 +294,7 @@ __device__ __forceinline__ ChanList ChannelLevelsScan(int2* nodes, const Area& a
 					if (HALF)
 						v = HalfAt(table, x, cc & 0xFF, cc >> 8);
 					else if (diff)
-						v = table[dbase - 513 * x];
+						v = kReducedByDiff ? table[dbase - 513 * x] : DiffAt(table, x, cc & 0xFF, cc >> 8);
 					else
 						v = table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
@@ -358,7 +369,7 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 		top = 0xFFFF;
 	const unsigned top16 = unsigned(top) & 0xFFFF;
 	const int rowSize = 1 << (2 * shift);
-	const bool diff = shift == 8 || byDiff;   /* DiffBase */
+	const bool diff = shift == 8 || (kReducedByDiff && byDiff);   /* DiffBase */
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
 	unsigned best = 0xFFFFFFFFu;
@@ -380,10 +391,11 @@ __device__ NEBC7_SHARED ChanList ChannelLevelsSingle(int2* nodes, const Area& ar
 				break;
 			if (chunkOn && ((mask >> (2 * j)) & 1))
 			{
-				const int dbase = DiffBase(cc, shift);
+				const int dbase = kReducedByDiff ? DiffBase(cc, shift) : 0;
 				auto term = [&](int e) {
 					const int x = e & 0xFFFF;
-					const unsigned v = diff ? table[dbase - 513 * x] : table[size_t(x) * rowSize + cc];
+					const unsigned v = diff ? (kReducedByDiff ? table[dbase - 513 * x] : DiffAt(table, x, cc & 0xFF, cc >> 8))
+					                        : table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
 				};
 				unsigned s = 0;
@@ -440,7 +452,7 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 	if (top > 0xFFFF)
 		top = 0xFFFF;
 	const int rowSize = 1 << (2 * bits);
-	const bool diff = bits == 8 || byDiff;   /* DiffBase */
+	const bool diff = bits == 8 || (kReducedByDiff && byDiff);   /* DiffBase */
 	const int towerSize = 1 << bits;
 	const int nu = UniqueValues(ar, count, offset, uniq, lane);
 
@@ -474,10 +486,11 @@ __device__ NEBC7_SHARED int EstimateChannelLevels(const Area& ar, const AreaInfo
 			{
 				/* cc = iL + lane stays in row iH (iL <= hL, iL - cH a multiple of 32) */
 				const int cc = iL + lane;
-				const int dbase = DiffBase(cc, bits);
+				const int dbase = kReducedByDiff ? DiffBase(cc, bits) : 0;
 				auto term = [&](int e) {
 					const int x = e & 0xFFFF;
-					const unsigned v = diff ? table[dbase - 513 * x] : table[size_t(x) * rowSize + cc];
+					const unsigned v = diff ? (kReducedByDiff ? table[dbase - 513 * x] : DiffAt(table, x, cc & 0xFF, cc >> 8))
+					                        : table[size_t(x) * rowSize + cc];
 					return unsigned(e >> 16) * v * v;
 				};
 				unsigned s = 0;

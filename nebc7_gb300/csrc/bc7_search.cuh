@@ -25,15 +25,7 @@ namespace nebc7 {
 
 constexpr bool kHasNormalPasses = true;
 
-/* Whether the scans read the reduced tables of 2- and 3-bit indices through
-   the 8-bit difference tables (DiffBase) or in the reference's per-x
-   layout.  The difference tables serve the full searches best; the compact
-   default-preset kernel, whose time goes to the Mode6Index2 refinement,
-   keeps the per-x layout (its translation unit sets 0). */
-#ifndef NEBC7_REDUCED_BY_DIFF
-#define NEBC7_REDUCED_BY_DIFF 1
-#endif
-constexpr bool kReducedByDiff = NEBC7_REDUCED_BY_DIFF != 0;
+
 constexpr int kBig = 0x7FFFFFFF;
 
 struct __align__(16) SearchState

@@ -96,6 +96,12 @@ std::atomic<uint64_t> gWork[kNumWorkCounters];
 
 extern "C" {
 
+/* OPTION_PCA for the encodes that follow (0 off, the default). */
+void nebc7_oracle_set_pca(int on)
+{
+	SetPca(on != 0);
+}
+
 /* The work counters (port_counters.h) since the last reset, in WorkCounter
    order; returns how many there are (0 in the plain build). */
 int nebc7_oracle_work(uint64_t* out, int reset)

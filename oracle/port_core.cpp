@@ -15,8 +15,16 @@
 
 namespace nebc7_oracle {
 
+static bool gPca = false;
+
+void SetPca(bool on)
+{
+	gPca = on;
+}
+
 void MakeConfig(Config& cfg, int denoise, int denoiseStep, bool doDraft, bool doNormal, bool doSlow, bool linearData)
 {
+	cfg.pca = gPca;
 	cfg.denoise = denoise;
 	cfg.denoiseStep = denoiseStep;
 	cfg.doDraft = doDraft;

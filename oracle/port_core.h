@@ -38,6 +38,7 @@ struct Config
 	int denoiseStep;   /* kDenoiseStep: 0 or 9 */
 	bool doDraft, doNormal, doSlow;
 	bool mode6Index2Only;   /* draft chain reduced to Mode6Index2 (no counterpart in the reference) */
+	bool pca;               /* OPTION_PCA: the principal-axis bounds of the full searches */
 	int wA, wG, wR, wB, wColor, wColorAlpha;
 	const LevelTables* lt;
 	const Selection* sel;
@@ -55,6 +56,11 @@ struct Config
 
 void MakeConfig(Config& cfg, int denoise, int denoiseStep, bool doDraft, bool doNormal, bool doSlow, bool linearData);
 
+/* OPTION_PCA for the configurations made after the call (off by default, as
+   in the reference's src/Bc7Mode.h:5). */
+void SetPca(bool on);
+
+
 /* src/Bc7Core.h:37 */
 struct Area
 {
@@ -67,6 +73,10 @@ struct Area
 	uint16_t minmax[8];    /* min, max per channel */
 	uint16_t bounds[8];    /* oriented endpoints per channel */
 };
+
+/* src/Bc7PcaEigen.cpp:26-146: the principal-axis error bound of an area over
+   G, R, B (C = 3) or A, G, R, B (C = 4); port_pca.cpp. */
+int PcaBound(const Config& cfg, const Area& area, int C);
 
 /* src/Bc7Core.h:55 */
 struct Cell

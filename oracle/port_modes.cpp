@@ -531,12 +531,13 @@ void FullTwoSubsets(const Config& cfg, const Opaque3Spec& s, const int* variants
 			continue;
 		GetArea(cfg, input.a12[p], input.lazy12[p], input, sel.sel12[p]);
 		const int water1 = input.errTotal - step - input.opaqueAlphaError;
-		const int line1 = 0; /* AreaGetBestPca3 without OPTION_PCA */
+		/* AreaGetBestPca3 (src/Bc7Core.cpp:494): 0 without OPTION_PCA */
+		const int line1 = cfg.pca ? PcaBound(cfg, input.a12[p], 3) : 0;
 		if (line1 < water1)
 		{
 			GetArea(cfg, input.a22[p], input.lazy22[p], input, sel.sel22[p]);
 			const int water2 = water1 - line1;
-			const int line2 = 0;
+			const int line2 = cfg.pca ? PcaBound(cfg, input.a22[p], 3) : 0;
 			if (line2 < water2)
 			{
 				lines1[p] = line1;
@@ -1890,7 +1891,8 @@ void Full(const Config& cfg, Cell& input)
 	if (input.personalMode == 6)
 		return;
 	const int step = input.denoiseStep;
-	const int line = 0; /* EstimateBest without OPTION_PCA */
+	/* EstimateBest (src/Bc7CoreMode6.cpp:1383-1396): 0 without OPTION_PCA */
+	const int line = cfg.pca ? PcaBound(cfg, input.area1, input.area1.opaque ? 3 : 4) : 0;
 	if (line < input.errTotal - step)
 	{
 		V8 mc = V8Zero();
@@ -2190,12 +2192,13 @@ void Full(const Config& cfg, Cell& input)
 			continue;
 		GetArea(cfg, input.a12[p], input.lazy12[p], input, sel.sel12[p]);
 		const int water1 = input.errTotal - step;
-		const int line1 = 0; /* EstimateBest without OPTION_PCA */
+		/* EstimateBest (src/Bc7CoreMode7.cpp:559-572): 0 without OPTION_PCA */
+		const int line1 = cfg.pca ? PcaBound(cfg, input.a12[p], input.a12[p].opaque ? 3 : 4) : 0;
 		if (line1 < water1)
 		{
 			GetArea(cfg, input.a22[p], input.lazy22[p], input, sel.sel22[p]);
 			const int water2 = water1 - line1;
-			const int line2 = 0;
+			const int line2 = cfg.pca ? PcaBound(cfg, input.a22[p], input.a22[p].opaque ? 3 : 4) : 0;
 			if (line2 < water2)
 			{
 				lines1[p] = line1;

@@ -47,6 +47,7 @@ class Port:
         L.nebc7_oracle_decompress_blocks.argtypes = [VP, VP, I]
         L.nebc7_oracle_prepare_texture.argtypes = [VP, I, I, VP, VP, I]
         L.nebc7_oracle_init.argtypes = [I]
+        L.nebc7_oracle_set_pca.argtypes = [I]
         L.nebc7_oracle_table.restype = VP
         L.nebc7_oracle_table.argtypes = [I, I, ctypes.POINTER(ctypes.c_int)]
         self.lib = L

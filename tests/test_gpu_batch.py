@@ -75,7 +75,7 @@ def test_every_plan_gives_the_plain_blocks(native, plan):
     """The tuner's knobs (schedule, staged form, CTAs per SM) change how the
     blocks are scheduled, never what they are."""
     torch = pytest.importorskip("torch")
-    texs = _textures(torch, 15, 53, 4, 96, ["precise", "default", "slow", "draft", "data"])
+    texs = _textures(torch, 15, 53, 4, 128, ["precise", "default", "slow", "draft", "data"])
     want = [_plain(native, torch, t) for t in texs]
     b = _batch(texs)
     b.set_plan(*plan)
