@@ -143,6 +143,18 @@ int nebc7_decode_device(const uint8_t* d_blocks, uint8_t* d_bgra, long long stri
 /* Decodes n blocks to 64 bytes of BGRA each (host buffers). */
 int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n);
 
+/* OPTION_PCA (src/Bc7Mode.h:5, off in the reference's build and here by
+   default): the full searches of modes 1, 3, 6 and 7 order and bound their
+   partitions by the principal-axis residual of each area
+   (PrincipalComponentAnalysis, src/Bc7PcaEigen.cpp:26-146; consumers
+   src/Bc7Core.cpp:494, src/Bc7CoreMode1.cpp:490-496, Mode3.cpp:488-494,
+   Mode6.cpp:1383-1396, Mode7.cpp:559-572).  Applies to encodes, batches and
+   servers created after the call.  The reference takes the axis from the
+   third-party Eigen 3.3.7, absent from its tree; the SVD here restates
+   Eigen's published JacobiSVD, so PCA-on outputs are not pinned to a PCA
+   build of the reference (they are tested against the CPU restatement). */
+int nebc7_set_pca(int on);
+
 /* How many kernels one nebc7_encode_device call with these settings
    launches (the block order, then the encode: one persistent kernel, or
    for the presets whose time goes to the full searches the staged form of

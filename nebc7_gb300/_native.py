@@ -162,6 +162,7 @@ SIGNATURES = {
     "nebc7_decode_blocks_host": (I, [VP, VP, I]),
     "nebc7_init_device": (I, [I]),
     "nebc7_encode_launches": (I, [ctypes.POINTER(Settings)]),
+    "nebc7_set_pca": (I, [I]),
     "nebc7_table_read": (I, [I, I, VP, LL, ctypes.POINTER(LL)]),
     "nebc7_launch_shape": (I, [VP, VP, VP]),
     "nebc7_encode_device_noalloc": (I, [VP, VP, VP, LL, I, I, ctypes.POINTER(Settings), VP, VP]),

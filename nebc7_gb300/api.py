@@ -225,6 +225,13 @@ def encode_image(img_bgra: np.ndarray, flags: str = "", preset: Preset = DEFAULT
     return EncodedImage(blocks, pw, ph, stats)
 
 
+def set_pca(on: bool) -> None:
+    """OPTION_PCA for the encodes, batches and servers created afterwards
+    (off by default, as in the reference's build; PCA-on outputs are not
+    pinned to the reference, whose axis comes from the absent Eigen)."""
+    check(_native.load().nebc7_set_pca(int(bool(on))), "set_pca")
+
+
 def encode_device(dst_ptr: int, bgra_ptr: int, mask_ptr: int | None, stride: int, width: int, height: int,
                   preset: Preset = DEFAULT, draft: bool = True, normal: bool = True, slow: bool = False,
                   linear: bool = False, stream: int = 0, want_stats: bool = False) -> EncodeStats | None:
@@ -422,6 +429,6 @@ class Server:
 
 __all__ = [
     "Bc7Core", "Preset", "DEFAULT", "PRECISE", "EncodeStats", "EncodedImage", "NativeError",
-    "encode_image", "encode_device", "pad_texture", "outline_mask", "padded_size", "parse_flags",
+    "encode_image", "encode_device", "set_pca", "pad_texture", "outline_mask", "padded_size", "parse_flags",
     "Batch", "BatchTexture", "Server", "ktx_header", "write_ktx", "read_ktx",
 ]

@@ -107,6 +107,7 @@ struct Params
 	int wA, wG, wR, wB;
 	int wColor, wColorAlpha;
 	int doDraft, doNormal, doSlow;
+	int pca;                    /* OPTION_PCA bounds in the full searches (off by default) */
 };
 
 template<int kD>

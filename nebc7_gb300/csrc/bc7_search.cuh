@@ -20,6 +20,7 @@
 
 #include "bc7_fast.cuh"
 #include "bc7_levels.cuh"
+#include "bc7_pca.cuh"
 
 namespace nebc7 {
 
@@ -560,64 +561,114 @@ __device__ NEBC7_PASS void FullThreeSubsets(WarpState& st, SearchState& ss, Cell
 	}
 }
 
+/* The partition search of modes 1 and 3 from its estimates (the second
+   loop of src/Bc7CoreMode1.cpp:473-571, src/Bc7CoreMode3.cpp:471-569):
+   partition p with the principal-axis bounds line1, line2 (0 without
+   OPTION_PCA).  Returns true when the search ends the full pass. */
+template<int kD, int MODE>
+__device__ __forceinline__ bool TwoSubsetsPartition(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const Spec3& sp,
+	const LevelTables& T, int p, int line1, int line2, int lane)
+{
+	const int step = R.denoiseStep;
+	Ep mc[2] = { 0, 0 };
+	int e1[4], e2[4];
+	const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 2, p, 0, lane);
+	const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
+	int w1 = R.errTotal - step - R.opaqueAlphaError - line2;
+	line1 = max(line1, EstimateLevels3<kD>(ss, st.sub[0], a1, P, sp, w1, e1, lane));
+	if (line1 < w1)
+	{
+		int w2 = w1 - line1;
+		line2 = max(line2, EstimateLevels3<kD>(ss, st.sub[1], a2, P, sp, w2, e2, lane));
+		if (line2 < w2)
+		{
+			w1 = R.errTotal - step - R.opaqueAlphaError - line2;
+			const int est1[3] = { e1[1], e1[2], e1[3] };
+			bool any;
+			int error = SearchSubset3<kD, MODE>(ss, st.sub[0], a1, P, T, w1, est1, mc[0], any, lane);
+			if (any && error < w1)
+			{
+				error += R.opaqueAlphaError;
+				w2 = R.errTotal - step - error;
+				const int est2[3] = { e2[1], e2[2], e2[3] };
+				const int r2 = SearchSubset3<kD, MODE>(ss, st.sub[1], a2, P, T, w2, est2, mc[1], any, lane);
+				if (any)
+				{
+					error += r2;
+					if (R.errTotal > error + step)
+					{
+						R.errTotal = error;
+						R.best[0] = mc[0];
+						R.best[1] = mc[1];
+						R.bestParam = p;
+						R.bestMode = MODE;
+						if (error <= R.opaqueAlphaError)
+							return true;
+					}
+				}
+			}
+		}
+	}
+	return false;
+}
+
 /* Full searches of modes 1 and 3 (src/Bc7CoreMode1.cpp:473-571,
-   src/Bc7CoreMode3.cpp:471-569); the PCA bound is zero in the reference's
-   default build. */
+   src/Bc7CoreMode3.cpp:471-569).  Without OPTION_PCA every partition's
+   bound is zero, so every partition enters with estimate OA + step and the
+   stable sort keeps index order; with it, the partitions are estimated and
+   sorted first (AreaGetBestPca3, src/Bc7Core.cpp:494). */
 template<int kD, int MODE>
 __device__ NEBC7_PASS void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
 {
 	const Spec3 sp = GetSpec3<MODE>(T);
 	const int step = R.denoiseStep;
-	/* every partition enters with estimate OA + step (ties keep index order) */
+	if (!P.pca)
+	{
+		for (int p = 0; p < 64; p++)
+		{
+			if (R.personalMode == MODE && R.personalParam == p)
+				continue;
+			if (!(0 < R.errTotal - step - R.opaqueAlphaError))
+				continue;
+			if (!(R.opaqueAlphaError + step < R.errTotal))
+				continue;
+			if (TwoSubsetsPartition<kD, MODE>(st, ss, R, P, sp, T, p, 0, 0, lane))
+				return;
+		}
+		return;
+	}
+	int count = 0;
 	for (int p = 0; p < 64; p++)
 	{
 		if (R.personalMode == MODE && R.personalParam == p)
 			continue;
-		const int water1 = R.errTotal - step - R.opaqueAlphaError;
-		if (!(0 < water1))
-			continue;
-		if (!(R.opaqueAlphaError + step < R.errTotal))
-			continue;
-		Ep mc[2] = { 0, 0 };
-		int e1[4], e2[4];
 		const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 2, p, 0, lane);
-		const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
-		int line1 = 0, line2 = 0;
-		int w1 = R.errTotal - step - R.opaqueAlphaError - line2;
-		line1 = max(line1, EstimateLevels3<kD>(ss, st.sub[0], a1, P, sp, w1, e1, lane));
-		if (line1 < w1)
+		const int water1 = R.errTotal - step - R.opaqueAlphaError;
+		const int line1 = PcaBound<kD>(st.sub[0], a1, P, 3, lane);
+		if (line1 < water1)
 		{
-			int w2 = w1 - line1;
-			line2 = max(line2, EstimateLevels3<kD>(ss, st.sub[1], a2, P, sp, w2, e2, lane));
-			if (line2 < w2)
+			const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
+			const int line2 = PcaBound<kD>(st.sub[1], a2, P, 3, lane);
+			if (line2 < water1 - line1)
 			{
-				w1 = R.errTotal - step - R.opaqueAlphaError - line2;
-				const int est1[3] = { e1[1], e1[2], e1[3] };
-				bool any;
-				int error = SearchSubset3<kD, MODE>(ss, st.sub[0], a1, P, T, w1, est1, mc[0], any, lane);
-				if (any && error < w1)
+				if (lane == 0)
 				{
-					error += R.opaqueAlphaError;
-					w2 = R.errTotal - step - error;
-					const int est2[3] = { e2[1], e2[2], e2[3] };
-					const int r2 = SearchSubset3<kD, MODE>(ss, st.sub[1], a2, P, T, w2, est2, mc[1], any, lane);
-					if (any)
-					{
-						error += r2;
-						if (R.errTotal > error + step)
-						{
-							R.errTotal = error;
-							R.best[0] = mc[0];
-							R.best[1] = mc[1];
-							R.bestParam = p;
-							R.bestMode = MODE;
-							if (error <= R.opaqueAlphaError)
-								return;
-						}
-					}
+					ss.lines[p][0] = line1;
+					ss.lines[p][1] = line2;
+					ss.order[count] = make_int2(R.opaqueAlphaError + line1 + line2 + step, p);
 				}
+				count++;
 			}
 		}
+		__syncwarp();
+	}
+	__syncwarp();
+	StableSortOrder(ss.order, count, lane);
+	for (int i = 0; i < count; i++)
+	{
+		const int2 o = ss.order[i];
+		if (o.x < R.errTotal && TwoSubsetsPartition<kD, MODE>(st, ss, R, P, sp, T, o.y, ss.lines[o.y][0], ss.lines[o.y][1], lane))
+			return;
 	}
 }
 
@@ -834,7 +885,9 @@ __device__ NEBC7_PASS void FullMode6(WarpState& st, SearchState& ss, CellRegs& R
 	if (R.personalMode == 6)
 		return;
 	const int step = R.denoiseStep;
-	if (0 < R.errTotal - step)
+	/* EstimateBest (src/Bc7CoreMode6.cpp:1383-1396): 0 without OPTION_PCA */
+	const int line = P.pca ? PcaBound<kD>(st.area1, R.a1, P, R.a1.opaque ? 3 : 4, lane) : 0;
+	if (line < R.errTotal - step)
 	{
 		Ep mc = 0;
 		const int error = CompressSubsetSingle<kD, 6>(ss, st.area1, R.a1, P, T, mc, R.errTotal - step, lane);
@@ -921,56 +974,115 @@ __device__ NEBC7_PASS int EstimateLevels7(SearchState& ss, const Area& ar, const
 	return water;
 }
 
+/* The partition search of mode 7 from its estimates (the second loop of
+   src/Bc7CoreMode7.cpp:629-725): partition p with the principal-axis bounds
+   line1, line2 (0 without OPTION_PCA).  Returns true when the search ends
+   the full pass. */
 template<int kD>
-__device__ NEBC7_PASS void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ __forceinline__ bool Mode7Partition(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T,
+	int p, int line1, int line2, int lane)
 {
-	/* src/Bc7CoreMode7.cpp:629-725; every partition enters with estimate step */
 	const int step = R.denoiseStep;
-	for (int p = 0; p < 64; p++)
+	Ep mc[2] = { 0, 0 };
+	int e1[4], e2[4];
+	const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 2, p, 0, lane);
+	const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
+	int w1 = R.errTotal - step - line2;
+	line1 = max(line1, EstimateLevels7<kD>(ss, st.sub[0], a1, P, T, w1, e1, lane));
+	if (line1 < w1)
 	{
-		if (R.personalMode == 7 && R.personalParam == p)
-			continue;
-		if (!(0 < R.errTotal - step))
-			continue;
-		if (!(step < R.errTotal))
-			continue;
-		Ep mc[2] = { 0, 0 };
-		int e1[4], e2[4];
-		const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 2, p, 0, lane);
-		const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
-		int line1 = 0, line2 = 0;
-		int w1 = R.errTotal - step - line2;
-		line1 = max(line1, EstimateLevels7<kD>(ss, st.sub[0], a1, P, T, w1, e1, lane));
-		if (line1 < w1)
+		int w2 = w1 - line1;
+		line2 = max(line2, EstimateLevels7<kD>(ss, st.sub[1], a2, P, T, w2, e2, lane));
+		if (line2 < w2)
 		{
-			int w2 = w1 - line1;
-			line2 = max(line2, EstimateLevels7<kD>(ss, st.sub[1], a2, P, T, w2, e2, lane));
-			if (line2 < w2)
+			w1 = R.errTotal - step - line2;
+			bool any;
+			int error = SearchSubset7<kD>(ss, st.sub[0], a1, P, T, w1, e1, mc[0], any, lane);
+			if (any && error < w1)
 			{
-				w1 = R.errTotal - step - line2;
-				bool any;
-				int error = SearchSubset7<kD>(ss, st.sub[0], a1, P, T, w1, e1, mc[0], any, lane);
-				if (any && error < w1)
+				w2 = R.errTotal - step - error;
+				const int r2 = SearchSubset7<kD>(ss, st.sub[1], a2, P, T, w2, e2, mc[1], any, lane);
+				if (any)
 				{
-					w2 = R.errTotal - step - error;
-					const int r2 = SearchSubset7<kD>(ss, st.sub[1], a2, P, T, w2, e2, mc[1], any, lane);
-					if (any)
+					error += r2;
+					if (R.errTotal > error + step)
 					{
-						error += r2;
-						if (R.errTotal > error + step)
-						{
-							R.errTotal = error;
-							R.best[0] = mc[0];
-							R.best[1] = mc[1];
-							R.bestParam = p;
-							R.bestMode = 7;
-							if (error <= 0)
-								return;
-						}
+						R.errTotal = error;
+						R.best[0] = mc[0];
+						R.best[1] = mc[1];
+						R.bestParam = p;
+						R.bestMode = 7;
+						if (error <= 0)
+							return true;
 					}
 				}
 			}
 		}
+	}
+	return false;
+}
+
+/* EstimateBest of mode 7 (src/Bc7CoreMode7.cpp:559-572): the principal-axis
+   bound over G, R, B for an opaque area, over A, G, R, B otherwise. */
+template<int kD>
+__device__ __forceinline__ int EstimateBest(const Area& ar, const AreaInfo& ai, const Params& P, int lane)
+{
+	return PcaBound<kD>(ar, ai, P, ai.opaque ? 3 : 4, lane);
+}
+
+template<int kD>
+__device__ NEBC7_PASS void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+{
+	/* src/Bc7CoreMode7.cpp:629-725; without OPTION_PCA every partition enters
+	   with estimate step (ties keep index order) */
+	const int step = R.denoiseStep;
+	if (!P.pca)
+	{
+		for (int p = 0; p < 64; p++)
+		{
+			if (R.personalMode == 7 && R.personalParam == p)
+				continue;
+			if (!(0 < R.errTotal - step))
+				continue;
+			if (!(step < R.errTotal))
+				continue;
+			if (Mode7Partition<kD>(st, ss, R, P, T, p, 0, 0, lane))
+				return;
+		}
+		return;
+	}
+	int count = 0;
+	for (int p = 0; p < 64; p++)
+	{
+		if (R.personalMode == 7 && R.personalParam == p)
+			continue;
+		const AreaInfo a1 = BuildSubset<kD>(st, R, P, st.sub[0], 2, p, 0, lane);
+		const int water1 = R.errTotal - step;
+		const int line1 = EstimateBest<kD>(st.sub[0], a1, P, lane);
+		if (line1 < water1)
+		{
+			const AreaInfo a2 = BuildSubset<kD>(st, R, P, st.sub[1], 2, p, 1, lane);
+			const int line2 = EstimateBest<kD>(st.sub[1], a2, P, lane);
+			if (line2 < water1 - line1)
+			{
+				if (lane == 0)
+				{
+					ss.lines[p][0] = line1;
+					ss.lines[p][1] = line2;
+					ss.order[count] = make_int2(line1 + line2 + step, p);
+				}
+				count++;
+			}
+		}
+		__syncwarp();
+	}
+	__syncwarp();
+	StableSortOrder(ss.order, count, lane);
+	for (int i = 0; i < count; i++)
+	{
+		const int2 o = ss.order[i];
+		if (o.x < R.errTotal && Mode7Partition<kD>(st, ss, R, P, T, o.y, ss.lines[o.y][0], ss.lines[o.y][1], lane))
+			return;
 	}
 }
 

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -159,9 +160,13 @@ int BuildTables(int dev, int denoise, const LevelTables** out)
 	return NEBC7_OK;
 }
 
+/* OPTION_PCA for the launches and plans made after nebc7_set_pca. */
+std::atomic<int> gPca{ 0 };
+
 Params MakeParams(const nebc7_settings& s)
 {
 	Params p;
+	p.pca = gPca.load();
 	p.denoiseStep = s.denoiseStep;
 	if (s.linearData)
 	{
@@ -1668,6 +1673,14 @@ int nebc7_decode_blocks_host(const uint8_t* blocks, uint8_t* bgra, int n)
 	cudaFree(db);
 	cudaFree(dp);
 	return rc;
+}
+
+int nebc7_set_pca(int on)
+{
+	if (on != 0 && on != 1)
+		return SetError(NEBC7_EINVAL);
+	gPca.store(on);
+	return NEBC7_OK;
 }
 
 int nebc7_encode_launches(const nebc7_settings* settings)

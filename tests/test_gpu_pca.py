@@ -1,0 +1,73 @@
+"""The OPTION_PCA build (GPU): with the principal-axis bounds on in both the
+CUDA encoder and the CPU restatement (oracle/port_pca.cpp), every block and
+sum is the same.
+
+The reference computes the axis with the third-party Eigen 3.3.7, which is
+absent from its tree; both sides here restate Eigen's published JacobiSVD,
+so this pins the GPU to the restatement, not to a PCA build of the
+reference ("parity unpinned").  PCA is off by default and switched off
+again after each test.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from nebc7_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+SSIM_RTOL = 1e-9
+
+
+@pytest.fixture
+def pca_on(native, port):
+    assert native.nebc7_set_pca(1) == 0
+    port.lib.nebc7_oracle_set_pca(1)
+    yield
+    native.nebc7_set_pca(0)
+    port.lib.nebc7_oracle_set_pca(0)
+
+
+@pytest.mark.parametrize("preset", [(1, 9, 1, 1, 1, 0), (0, 0, 1, 1, 1, 0), (1, 9, 1, 1, 1, 1)])
+def test_pca_blocks_match_restatement(native, port, pca_on, preset):
+    from nebc7_gb300._native import Settings
+    n = 1200
+    cells, masks = synth.random_blocks(n, 4321)
+    a = np.zeros((n, 16), np.uint8)
+    b = np.zeros((n, 16), np.uint8)
+    e1, s1 = port.compress_blocks(cells, masks, a, *preset, threads=16)
+    err = np.zeros(2, np.int64)
+    ssim = np.zeros(2, np.float64)
+    assert native.nebc7_encode_blocks_host(cells.ctypes.data, masks.ctypes.data, b.ctypes.data, n,
+                                           ctypes.byref(Settings(*preset)), err.ctypes.data, ssim.ctypes.data) == 0
+    bad = np.nonzero((a != b).any(1))[0]
+    assert len(bad) == 0, f"{len(bad)} blocks differ, first {bad[:8].tolist()}"
+    assert e1.tolist() == err.tolist()
+    assert np.allclose(s1, ssim, rtol=SSIM_RTOL, atol=0)
+
+
+def test_pca_image_matches_restatement(native, port, pca_on):
+    from nebc7_gb300 import Preset, encode_image
+    img = synth.image_for("alpha_blobs", 96, 64, 19)
+    enc = encode_image(img, "/noflip /slow", Preset(1, 9))
+    padded, mask = port.prepare(img, 1)
+    out = np.zeros_like(enc.blocks)
+    err, _ = port.compress_texture(out, padded, mask, 1, 9, 1, 1, 1, 0, threads=16)
+    assert np.array_equal(out, enc.blocks)
+    assert err.tolist() == [enc.stats.err_alpha, enc.stats.err_color]
+
+
+def test_pca_changes_the_search(native, port):
+    """The switch takes effect: the restatement's /slow output on these
+    blocks differs with the bounds on (and PCA is off again afterwards)."""
+    cells, masks = synth.random_blocks(400, 77)
+    outs = []
+    for on in (0, 1, 0):
+        port.lib.nebc7_oracle_set_pca(on)
+        io = np.zeros((400, 16), np.uint8)
+        port.compress_blocks(cells, masks, io, 1, 9, 1, 1, 1, 0, threads=16)
+        outs.append(io)
+    assert not np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[2])
