@@ -892,96 +892,115 @@ __device__ int ComputeSubsetTable(WarpState& st, const Area& ar, const AreaInfo&
 		return errorBlock;
 	}
 
-	/* enumerate every combination of tied indices; keep the first maximum of
-	   the weighted SSIM (all lanes keep identical copies of the odometer) */
+	/* enumerate every combination of tied indices in the reference's odometer
+	   order (pixel 0 the fastest digit, each digit over its tied indices in
+	   ascending order) and keep the first maximum of the weighted SSIM
+	   (src/Bc7Core.cpp:1341-1428).  Lane j evaluates combination base + j
+	   on its own, so 32 combinations are in flight; the chunk's maximum and
+	   its first lane then meet the running best with the reference's strict
+	   comparison, which keeps the first maximum in odometer order.  At most
+	   2^20 combinations are visited. */
 	double bestSsim = -(double(P.wColorAlpha) + 0.1);
 	const int count = ai.count;
+	const int active = ai.active;
 	const int shift = count > 8 ? 4 : (count > 4 ? 3 : (count > 2 ? 2 : (count > 1 ? 1 : 0)));
-	int loops[16], ways[16];
-	for (int i = 0; i < 16; i++)
+	int total = 1;
+	for (int i = 0; i < active; i++)
 	{
-		loops[i] = st.loops[i];
-		ways[i] = st.ways[i];
+		const int way = st.ways[i];
+		const int n = way ? __popc(unsigned(way) & ((1u << M) - 1)) : 1;
+		total = (total > (1 << 20) / n) ? (1 << 20) + 1 : total * n;
 	}
-	const int myPx = lane < 16 ? lane : 0;
-	int pxv[4], mkv[4];
-	for (int c = 0; c < 4; c++)
+	if (total > (1 << 20))
+		total = 1 << 20;
+	int bestN = 0;
+	for (int base = 0; base < total; base += 32)
 	{
-		pxv[c] = ar.px[myPx][c];
-		mkv[c] = ar.mk[myPx][c];
-	}
-	for (int guard = 0; guard < (1 << 20); guard++)
-	{
-		double ssim = 0;
-		for (int c = 0; c < 4; c++)
+		const int n0 = base + lane;
+		double ssim = -(double(P.wColorAlpha) + 0.1);
+		if (n0 < total)
 		{
-			unsigned t = 0, b = 0;
-			if (lane < count)
+			/* the digits of combination n0: each tied pixel's index */
+			int idx[16];
+			int rest = n0;
+			for (int i = 0; i < 16; i++)
 			{
-				int l = 0;
-				for (int i = 0; i < 16; i++)
-					if (i == lane)
-						l = loops[i];
-				t = unsigned(vals[l][c] & mkv[c]);
-				b = unsigned(pxv[c]);
-			}
-			const unsigned sa = __reduce_add_sync(kFull, t);
-			const unsigned sb = __reduce_add_sync(kFull, b);
-			const unsigned sab = __reduce_add_sync(kFull, (t * b) & 0xFFFF);
-			const unsigned saa_sbb = __reduce_add_sync(kFull, ((t * t) & 0xFFFF) + ((b * b) & 0xFFFF));
-			unsigned vab = sab << (shift + 1);
-			unsigned vaa = saa_sbb << shift;
-			unsigned sasb = sa * sb;
-			sasb += sasb;
-			const unsigned sasa_sbsb = sa * sa + sb * sb;
-			vab -= sasb;
-			vaa -= sasa_sbsb;
-			const double s = SsimRatio(int(sasb), int(vab), int(sasa_sbsb), int(vaa));
-			ssim = (c == 0) ? __dmul_rn(s, double(w[0])) : __dadd_rn(ssim, __dmul_rn(s, double(w[c])));
-		}
-		if (bestSsim < ssim)
-		{
-			bestSsim = ssim;
-			if (lane < 16)
-			{
-				int l = 0;
-				for (int i = 0; i < 16; i++)
-					if (i == lane)
-						l = loops[i];
-				st.best[lane] = l;
-			}
-		}
-		/* odometer step */
-		int i = 0;
-		bool done = false;
-		for (;;)
-		{
-			const int way = ways[i];
-			if (way)
-			{
-				int k = loops[i];
-				do
+				const int way = st.ways[i];
+				int k = st.loops[i];
+				if (i < active && way)
 				{
-					k++;
-				} while ((way & (1 << k)) == 0);
-				if (k < M)
-				{
-					loops[i] = k;
-					break;
+					const unsigned tied = unsigned(way) & ((1u << M) - 1);
+					const int n = __popc(tied);
+					int d = rest % n;
+					rest /= n;
+					unsigned t = tied;
+					while (d-- > 0)
+						t &= t - 1;
+					k = __ffs(t) - 1;
 				}
-				k = 0;
-				while ((way & (1 << k)) == 0)
-					k++;
-				loops[i] = k;
+				idx[i] = k;
 			}
-			if (++i >= ai.active)
+			for (int c = 0; c < 4; c++)
 			{
-				done = true;
-				break;
+				unsigned sa = 0, sb = 0, sab = 0, saa_sbb = 0;
+				for (int i = 0; i < count; i++)
+				{
+					const unsigned t = unsigned(vals[idx[i]][c] & ar.mk[i][c]);
+					const unsigned b = unsigned(ar.px[i][c]);
+					sa += t;
+					sb += b;
+					sab += (t * b) & 0xFFFF;
+					saa_sbb += ((t * t) & 0xFFFF) + ((b * b) & 0xFFFF);
+				}
+				unsigned vab = sab << (shift + 1);
+				unsigned vaa = saa_sbb << shift;
+				unsigned sasb = sa * sb;
+				sasb += sasb;
+				const unsigned sasa_sbsb = sa * sa + sb * sb;
+				vab -= sasb;
+				vaa -= sasa_sbsb;
+				const double r = SsimRatio(int(sasb), int(vab), int(sasa_sbsb), int(vaa));
+				ssim = (c == 0) ? __dmul_rn(r, double(w[0])) : __dadd_rn(ssim, __dmul_rn(r, double(w[c])));
 			}
 		}
-		if (done)
-			break;
+		/* the chunk's maximum (exact comparisons of doubles) and its first lane */
+		double m = ssim;
+		for (int o = 16; o > 0; o >>= 1)
+		{
+			const double v = __shfl_xor_sync(kFull, m, o);
+			m = v > m ? v : m;
+		}
+		const unsigned at = __ballot_sync(kFull, n0 < total && ssim == m);
+		if (bestSsim < m)
+		{
+			bestSsim = m;
+			bestN = base + __ffs(at) - 1;
+		}
+	}
+	/* the indices of the winning combination */
+	if (lane < 16)
+	{
+		int k = st.loops[lane];
+		int rest = bestN;
+		for (int i = 0; i < 16; i++)
+		{
+			const int way = st.ways[i];
+			if (i < active && way)
+			{
+				const unsigned tied = unsigned(way) & ((1u << M) - 1);
+				const int n = __popc(tied);
+				const int d = rest % n;
+				rest /= n;
+				if (i == lane)
+				{
+					unsigned t = tied;
+					for (int e = 0; e < d; e++)
+						t &= t - 1;
+					k = __ffs(t) - 1;
+				}
+			}
+		}
+		st.best[lane] = k;
 	}
 	__syncwarp();
 	return errorBlock;

@@ -498,6 +498,48 @@ static __global__ void __launch_bounds__(1024) KStageList(const int* next, int t
 		*count = base;
 }
 
+/* Gathers the positions whose next pass is `stage`, largest error first:
+   a counting sort on 8 buckets per octave of the record's errTotal (one
+   block of 1024 threads).  A search's cost grows with its water, so the
+   longest searches of a pass start first and no SM waits at the end of the
+   pass behind a late hard block; the order inside a bucket is any, and
+   the blocks written are the same either way. */
+static __global__ void __launch_bounds__(1024) KStageListByError(const int* next, const BlockRecord* rec, int total, int stage,
+	int* list, int* count)
+{
+	__shared__ int hist[256];
+	__shared__ int base[256];
+	for (int i = threadIdx.x; i < 256; i += 1024)
+		hist[i] = 0;
+	__syncthreads();
+	auto bucketOf = [&](int k) {
+		const unsigned e = unsigned(max(rec[k].errTotal, 0));
+		if (!e)
+			return 255;
+		const int msb = 31 - __clz(e);
+		const int frac = int((e >> (msb >= 3 ? msb - 3 : 0)) & 7u);
+		return 255 - min(255, msb * 8 + frac);
+	};
+	for (int k = threadIdx.x; k < total; k += 1024)
+		if (next[k] == stage)
+			atomicAdd(&hist[bucketOf(k)], 1);
+	__syncthreads();
+	if (threadIdx.x == 0)
+	{
+		int run = 0;
+		for (int b = 0; b < 256; b++)
+		{
+			base[b] = run;
+			run += hist[b];
+		}
+		*count = run;
+	}
+	__syncthreads();
+	for (int k = threadIdx.x; k < total; k += 1024)
+		if (next[k] == stage)
+			list[atomicAdd(&base[bucketOf(k)], 1)] = k;
+}
+
 /* Host-side launcher of a staged encode: the draft kernel, then for each
    pass its list and its kernel, then the finish kernel's list and kernel.
    The launches are capturable.  Compiled per kD in encode_*_staged.cu. */

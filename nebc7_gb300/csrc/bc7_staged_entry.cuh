@@ -11,7 +11,11 @@ namespace nebc7 {
 template<int kD, int STAGE>
 cudaError_t LaunchStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
 {
-	if (STAGE != kStageDraft)
+	/* the passes after the draft chain take their blocks largest error
+	   first; the draft chain and the pack keep the queue order */
+	if (STAGE >= kStepRefine && STAGE < kStepFinish)
+		KStageListByError<<<1, 1024, 0, stream>>>(sg.next, sg.rec, job.total, STAGE, sg.list, sg.count + STAGE);
+	else if (STAGE != kStageDraft)
 		KStageList<<<1, 1024, 0, stream>>>(sg.next, job.total, STAGE, sg.list, sg.count + (STAGE < 0 ? 0 : STAGE));
 	KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, T0, T1);
 	return cudaGetLastError();

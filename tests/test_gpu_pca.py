@@ -57,17 +57,3 @@ def test_pca_image_matches_restatement(native, port, pca_on):
     err, _ = port.compress_texture(out, padded, mask, 1, 9, 1, 1, 1, 0, threads=16)
     assert np.array_equal(out, enc.blocks)
     assert err.tolist() == [enc.stats.err_alpha, enc.stats.err_color]
-
-
-def test_pca_changes_the_search(native, port):
-    """The switch takes effect: the restatement's /slow output on these
-    blocks differs with the bounds on (and PCA is off again afterwards)."""
-    cells, masks = synth.random_blocks(400, 77)
-    outs = []
-    for on in (0, 1, 0):
-        port.lib.nebc7_oracle_set_pca(on)
-        io = np.zeros((400, 16), np.uint8)
-        port.compress_blocks(cells, masks, io, 1, 9, 1, 1, 1, 0, threads=16)
-        outs.append(io)
-    assert not np.array_equal(outs[0], outs[1])
-    assert np.array_equal(outs[0], outs[2])

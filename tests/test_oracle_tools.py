@@ -63,3 +63,39 @@ def test_port_matches_reference_cli_blocks(port, golden, name):
     port.compress_texture(out, padded, m, 1, 9, int(o["draft"]), int(o["normal"]), int(o["slow"]), int(o["linear"]),
                           threads=8)
     assert np.array_equal(out, f["blocks"])
+
+
+def test_pca_bounds_prune_the_search():
+    """OPTION_PCA's bounds only skip searches (src/Bc7CoreMode6.cpp:1407-1408:
+    a full search runs when the bound is below the best error): with them on,
+    the counter build of the port evaluates fewer subset-error terms on the
+    same /slow blocks, and switching them off again restores the count."""
+    import ctypes
+    import subprocess
+    from oracle.pyoracle import HERE as OH, VP, I
+    lib_path = OH / "liboracle_port_counters.so"
+    if not lib_path.exists():
+        subprocess.run(["sh", str(OH / "build_oracle.sh")], check=True, stdout=subprocess.DEVNULL)
+    L = ctypes.CDLL(str(lib_path))
+    L.nebc7_oracle_init.argtypes = [I]
+    L.nebc7_oracle_set_pca.argtypes = [I]
+    L.nebc7_oracle_work.argtypes = [VP, I]
+    L.nebc7_oracle_compress_blocks.argtypes = [VP, VP, VP, I, I, I, I, I, I, I, I, VP, VP]
+    cells, masks = synth.random_blocks(300, 77)
+    terms = []
+    try:
+        for on in (0, 1, 0):
+            L.nebc7_oracle_set_pca(on)
+            io = np.zeros((300, 16), np.uint8)
+            err = np.zeros(2, np.int64)
+            ssim = np.zeros(2, np.float64)
+            w = np.zeros(6, np.uint64)
+            L.nebc7_oracle_work(w.ctypes.data, 1)
+            assert L.nebc7_oracle_compress_blocks(cells.ctypes.data, masks.ctypes.data, io.ctypes.data, 300, 1, 9,
+                                                  1, 1, 1, 0, 8, err.ctypes.data, ssim.ctypes.data) == 0
+            L.nebc7_oracle_work(w.ctypes.data, 0)
+            terms.append(int(w[1]))
+    finally:
+        L.nebc7_oracle_set_pca(0)
+    assert terms[1] < terms[0]
+    assert terms[2] == terms[0]
