@@ -616,15 +616,18 @@ __device__ __forceinline__ bool TwoSubsetsPartition(WarpState& st, SearchState& 
    src/Bc7CoreMode3.cpp:471-569).  Without OPTION_PCA every partition's
    bound is zero, so every partition enters with estimate OA + step and the
    stable sort keeps index order; with it, the partitions are estimated and
-   sorted first (AreaGetBestPca3, src/Bc7Core.cpp:494). */
+   sorted first (AreaGetBestPca3, src/Bc7Core.cpp:494).  Without OPTION_PCA
+   the search may resume at partition `from` (the partitions before it
+   searched already, R as they left it). */
 template<int kD, int MODE>
-__device__ NEBC7_PASS void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullTwoSubsets(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane,
+	int from = 0)
 {
 	const Spec3 sp = GetSpec3<MODE>(T);
 	const int step = R.denoiseStep;
 	if (!P.pca)
 	{
-		for (int p = 0; p < 64; p++)
+		for (int p = from; p < 64; p++)
 		{
 			if (R.personalMode == MODE && R.personalParam == p)
 				continue;
@@ -1031,14 +1034,16 @@ __device__ __forceinline__ int EstimateBest(const Area& ar, const AreaInfo& ai, 
 }
 
 template<int kD>
-__device__ NEBC7_PASS void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullMode7(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane,
+	int from = 0)
 {
 	/* src/Bc7CoreMode7.cpp:629-725; without OPTION_PCA every partition enters
-	   with estimate step (ties keep index order) */
+	   with estimate step (ties keep index order), and the search may resume
+	   at partition `from` */
 	const int step = R.denoiseStep;
 	if (!P.pca)
 	{
-		for (int p = 0; p < 64; p++)
+		for (int p = from; p < 64; p++)
 		{
 			if (R.personalMode == 7 && R.personalParam == p)
 				continue;
@@ -1270,12 +1275,14 @@ __device__ NEBC7_PASS void RefineMode5(WarpState& st, SearchState& ss, CellRegs&
 }
 
 template<int kD, int MODE>
-__device__ NEBC7_PASS void FullRot(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ NEBC7_PASS void FullRot(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane,
+	int from = 0)
 {
-	/* src/Bc7CoreMode4.cpp:1824-1857, src/Bc7CoreMode5.cpp:913-946 */
+	/* src/Bc7CoreMode4.cpp:1824-1857, src/Bc7CoreMode5.cpp:913-946; the
+	   search may resume at choice `from` */
 	const int step = R.denoiseStep;
 	constexpr int NR = MODE == 4 ? 8 : 4;
-	for (int ri = 0; ri < NR; ri++)
+	for (int ri = from; ri < NR; ri++)
 	{
 		const int rotation = MODE == 4 ? c_rot4[ri] : c_rot5[ri];
 		if (MODE == 4 && R.personalMode == 4 && !((R.personalParam ^ rotation) & 3))

@@ -17,10 +17,25 @@
  * endpoints, mode, partition, errors, stepping values, the starting block)
  * is kept in a BlockRecord per queue position; the pixel data and the
  * whole-block area are rebuilt from the texture when a pass starts.  Each
- * pass kernel runs the blocks whose next pass it is, in queue order (widest
- * pixel range first), gathered by KStageList.  The passes, their order and
- * their entry conditions are those of NormalPasses, so the blocks are the
- * same bits as the single-kernel encode's.
+ * pass kernel runs the blocks whose next pass it is, gathered by
+ * KStageList (queue order) or KStageListByError (largest error first).
+ * The passes, their order and their entry conditions are those of
+ * NormalPasses, so the blocks are the same bits as the single-kernel
+ * encode's.
+ *
+ * The full searches of modes 1, 3 and 7 (64 two-subset partitions each)
+ * and of modes 4 and 5 (8 and 4 rotation / index-size choices) are split
+ * passes: a few hard blocks take most of their time, and one warp per block
+ * would leave the GPU waiting for them.  A split pass runs in rounds.  In a
+ * round every candidate (partition or rotation) of every block in the
+ * round's list is a task of its own, taken by any warp, searched from the
+ * block's error at the start of the round.  The candidates before a block's
+ * first improving candidate f searched from that error, as the reference's
+ * loop does, so their verdicts stand; f's result is the reference's too.
+ * The round's commit applies f and ends the pass, or the block continues
+ * in the next round from candidate f + 1 with the new error.  Improvements
+ * are rare, so most blocks finish in the first round; blocks still
+ * searching after kSplitRounds rounds finish their pass in one warp each.
  */
 #pragma once
 
@@ -60,8 +75,42 @@ struct __align__(16) BlockRecord
 	int bestParam, bestMode, opaqueAlphaError, errAlpha;
 	int errTotal, personalParam, personalMode, denoiseStep;
 	int water;                   /* the error at the start of the draft chain */
-	int pad[3];
+	int opaque;                  /* the whole-block area's opaque flag */
+	int pad[2];
 };
+
+/* An improving candidate of a split pass: its endpoints, error and
+   parameter (partition or rotation), and whether it ends the full search
+   (src/Bc7CoreMode1.cpp:563-564, src/Bc7CoreMode7.cpp:719-720,
+   src/Bc7CoreMode4.cpp:1852-1853). */
+struct __align__(16) SplitResult
+{
+	Ep best0, best1;
+	int error, end, param;
+	int pad;
+};
+
+/* The split passes and their rounds. */
+constexpr int kSplitRounds = 3;
+constexpr int kSplitMaxBlocks = 1 << 24;    /* blocks of a round split into partition tasks (the task count stays an int) */
+constexpr int kSplitSerial = -1;            /* firstImp: the block's pass runs whole (OPTION_PCA) */
+constexpr int kSplitNone = 0x7FFFFFFF;      /* firstImp: no improvement yet */
+
+__host__ __device__ constexpr int SplitIndex(int S)
+{
+	return S == kStepFull2Mode1 ? 0 : (S == kStepFull2Mode3 ? 1 : (S == kStepRot5 ? 2 : (S == kStepRot4 ? 3 : (S == kStepMode7 ? 4 : -1))));
+}
+
+/* Candidates (tasks) per block of split pass S, and its mode. */
+__host__ __device__ constexpr int SplitTasks(int S)
+{
+	return S == kStepRot4 ? 8 : (S == kStepRot5 ? 4 : 64);
+}
+
+__host__ __device__ constexpr int SplitMode(int S)
+{
+	return S == kStepFull2Mode1 ? 1 : (S == kStepFull2Mode3 ? 3 : (S == kStepRot5 ? 5 : (S == kStepRot4 ? 4 : 7)));
+}
 
 /* Per-launch state of a staged encode (one entry per queue position). */
 struct Stages
@@ -71,6 +120,13 @@ struct Stages
 	int* list;        /* positions of the pass being run, in queue order */
 	int* count;       /* [kNumStages] list lengths */
 	int* counters;    /* [kNumStages + 1] work-queue heads, zero before the draft kernel */
+	/* split passes */
+	int* start;       /* per position: the first candidate of the block's next round */
+	int* firstImp;    /* per position: (candidate << 24) | result slot of the round's first improvement */
+	int* splitList[3];   /* the lists of rounds 1 and 2 and of the one-warp remainder */
+	int* split;       /* [5 split passes][4][4] list lengths, task heads, result counts; zero before the draft kernel */
+	SplitResult* imp;
+	int impCap;
 };
 
 __device__ __forceinline__ void SaveRecord(BlockRecord& r, const CellRegs& R, int lane)
@@ -88,6 +144,7 @@ __device__ __forceinline__ void SaveRecord(BlockRecord& r, const CellRegs& R, in
 		r.personalParam = R.personalParam;
 		r.personalMode = R.personalMode;
 		r.denoiseStep = R.denoiseStep;
+		r.opaque = R.a1.opaque;
 	}
 }
 
@@ -116,7 +173,8 @@ __device__ __forceinline__ void RestoreBlock(WarpState& st, CellRegs& R, const B
 /* One stage: passes of the draft chain after the mode 6 fast pass
    (DraftChain), or one pass of the normal / slow chains (NormalPasses). */
 template<int kD, int S>
-__device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane)
+__device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs& R, const Params& P, const LevelTables& T, int lane,
+	int from = 0)
 {
 	if constexpr (S == kStepDraftRot)
 	{
@@ -163,15 +221,15 @@ __device__ __forceinline__ void RunStep(WarpState& st, SearchState& ss, CellRegs
 	else if constexpr (S == kStepFull3Mode0)
 		FullThreeSubsets<kD, 0>(st, ss, R, P, T, lane);
 	else if constexpr (S == kStepFull2Mode1)
-		FullTwoSubsets<kD, 1>(st, ss, R, P, T, lane);
+		FullTwoSubsets<kD, 1>(st, ss, R, P, T, lane, from);
 	else if constexpr (S == kStepFull2Mode3)
-		FullTwoSubsets<kD, 3>(st, ss, R, P, T, lane);
+		FullTwoSubsets<kD, 3>(st, ss, R, P, T, lane, from);
 	else if constexpr (S == kStepRot5)
-		FullRot<kD, 5>(st, ss, R, P, T, lane);
+		FullRot<kD, 5>(st, ss, R, P, T, lane, from);
 	else if constexpr (S == kStepRot4)
-		FullRot<kD, 4>(st, ss, R, P, T, lane);
+		FullRot<kD, 4>(st, ss, R, P, T, lane, from);
 	else if constexpr (S == kStepMode7)
-		FullMode7<kD>(st, ss, R, P, T, lane);
+		FullMode7<kD>(st, ss, R, P, T, lane, from);
 	else if constexpr (S == kStepMode6)
 		FullMode6<kD>(st, ss, R, P, T, lane);
 }
@@ -366,14 +424,15 @@ __device__ bool DraftStage(WarpState& st, const BlockRef& b, const LevelTables& 
 	return false;
 }
 
-/* A pass kernel's block: runs pass S and records the next one. */
+/* A pass kernel's block: runs pass S (of a split pass, the partitions from
+   `from` on) and records the next one. */
 template<int kD, int S>
 __device__ void PassStage(WarpState& st, SearchState& ss, const BlockRef& b, const LevelTables& T, const Params& P, BlockRecord& rec,
-	int& next, int lane)
+	int& next, int from, int lane)
 {
 	CellRegs R;
 	RestoreBlock(st, R, b, rec, P, lane);
-	RunStep<kD, S>(st, ss, R, P, T, lane);
+	RunStep<kD, S>(st, ss, R, P, T, lane, from);
 	const int n = NextStep(S, R, P);
 	SaveRecord(rec, R, lane);
 	if (lane == 0)
@@ -405,33 +464,34 @@ __device__ __forceinline__ bool StageBlock(WarpState& st, SearchState& ss, const
 	}
 	else
 	{
-		PassStage<kD, STAGE>(st, ss, b, T, P, sg.rec[k], sg.next[k], lane);
+		PassStage<kD, STAGE>(st, ss, b, T, P, sg.rec[k], sg.next[k], SplitIndex(STAGE) >= 0 ? sg.start[k] : 0, lane);
 		return false;
 	}
 }
 
-/* One stage of a staged encode over the launch's queue: the draft kernel
-   takes every position; a pass or the finish kernel takes the positions
-   KStageList gathered for it.  kD as for KEncode. */
+/* One stage of a staged encode over a list of queue positions (`list`,
+   *count entries, taken through *head): the draft kernel takes every
+   position (no list); a pass or the finish kernel takes the positions
+   gathered for it.  kD as for KEncode. */
 template<int kD, int STAGE>
-__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeStage(Job job, Stages sg, LevelTables T0, LevelTables T1)
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeStage(Job job, Stages sg, const int* list, const int* count, int* head,
+	LevelTables T0, LevelTables T1)
 {
 	extern __shared__ __align__(16) unsigned char encodeSmem[];
 	const int lane = threadIdx.x & 31;
 	const int warp = threadIdx.x >> 5;
 	WarpState& st = reinterpret_cast<WarpState*>(encodeSmem)[warp];
 	SearchState& ss = reinterpret_cast<SearchState*>(encodeSmem + kWarpsPerCta * sizeof(WarpState))[warp];
-	const int n = STAGE == kStageDraft ? job.total : sg.count[STAGE < 0 ? 0 : STAGE];
-	int* counter = sg.counters + (STAGE + 1);
+	const int n = list ? *count : job.total;
 	for (;;)
 	{
 		int i = 0;
 		if (lane == 0)
-			i = atomicAdd(counter, 1);
+			i = atomicAdd(head, 1);
 		i = __shfl_sync(kFull, i, 0);
 		if (i >= n)
 			break;
-		const int k = STAGE == kStageDraft ? i : sg.list[i];
+		const int k = list ? list[i] : i;
 		TexDesc d;
 		BlockRef b;
 		QueuedBlock(job, k, d, b);
@@ -448,6 +508,237 @@ __global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeStage(Job job, St
 			finished = StageBlock<kD, STAGE>(st, ss, b, kD ? T1 : T0, P, sg, k, lane);
 		if (finished)
 			BlockFinished(d, lane);
+	}
+}
+
+/* One task of a split pass: candidate p of the block at position k,
+   searched from the error in its record (the error at the start of the
+   round).  An improving candidate before the round's first improvement so
+   far keeps its result and lowers the block's firstImp; a candidate after
+   it is not searched (the next round searches it again). */
+template<int kD, int S>
+__device__ NEBC7_PASS void SplitTask(WarpState& st, SearchState& ss, const BlockRef& b, const LevelTables& T, const Params& P,
+	const Stages& sg, int* impCount, int k, int p, int lane)
+{
+	constexpr int MODE = SplitMode(S);
+	volatile int* first = sg.firstImp + k;
+	/* one read for the whole warp: other warps lower it meanwhile */
+	int firstNow = 0;
+	if (lane == 0)
+		firstNow = *first;
+	if ((__shfl_sync(kFull, firstNow, 0) >> 24) < p)
+		return;
+	CellRegs R;
+	RestoreBlock(st, R, b, sg.rec[k], P, lane);
+	const int E = R.errTotal, step = R.denoiseStep;
+	bool end;
+	int param = p;
+	/* the conditions of the candidate loops (FullTwoSubsets, FullMode7, FullRot) */
+	if constexpr (MODE == 4 || MODE == 5)
+	{
+		const int rotation = MODE == 4 ? c_rot4[p] : c_rot5[p];
+		if (MODE == 4 && R.personalMode == 4 && !((R.personalParam ^ rotation) & 3))
+			return;
+		if (MODE == 5 && R.personalMode == 5 && R.personalParam == rotation)
+			return;
+		Ep mc = 0;
+		int error = step;
+		if (error < E)
+			error += CompressRotSubset<kD, MODE>(st, ss, R, P, T, mc, E - error, rotation, lane);
+		if (!(E > error))
+			return;
+		R.errTotal = error - step;
+		R.best[0] = mc;
+		end = error <= step;
+		param = rotation;
+	}
+	else
+	{
+		if (R.personalMode == MODE && R.personalParam == p)
+			return;
+		if constexpr (MODE == 7)
+		{
+			if (!(0 < E - step) || !(step < E))
+				return;
+			end = Mode7Partition<kD>(st, ss, R, P, T, p, 0, 0, lane);
+		}
+		else
+		{
+			const int OA = R.opaqueAlphaError;
+			if (!(0 < E - step - OA) || !(OA + step < E))
+				return;
+			end = TwoSubsetsPartition<kD, MODE>(st, ss, R, P, GetSpec3<MODE>(T), T, p, 0, 0, lane);
+		}
+		if (R.errTotal == E)
+			return;
+	}
+	if (lane != 0 || (*first >> 24) < p)
+		return;
+	int slot = 0xFFFFFF;
+	const int at = atomicAdd(impCount, 1);
+	if (at < sg.impCap)
+	{
+		SplitResult r;
+		r.best0 = R.best[0];
+		r.best1 = R.best[1];
+		r.error = R.errTotal;
+		r.end = end;
+		r.param = param;
+		r.pad = 0;
+		sg.imp[at] = r;
+		slot = at;
+	}
+	atomicMin(sg.firstImp + k, (p << 24) | slot);
+}
+
+/* A round of split pass S over the blocks list[i], i < *count: the first
+   nSplit blocks as tasks (block, candidate p) for p from the block's start
+   candidate, taken through *head block by block, so that the candidates of
+   a block go to as many warps; the blocks after them (with more blocks than
+   the task count can number) as one task each, the whole pass in one warp
+   (PassStage). */
+template<int kD, int S>
+__global__ void __launch_bounds__(kWarpsPerCta * 32, 4) KEncodeSplit(Job job, Stages sg, const int* list, const int* count, int* head,
+	int* impCount, int nSplit, LevelTables T0, LevelTables T1)
+{
+	constexpr int NT = SplitTasks(S);
+	extern __shared__ __align__(16) unsigned char encodeSmem[];
+	const int lane = threadIdx.x & 31;
+	const int warp = threadIdx.x >> 5;
+	WarpState& st = reinterpret_cast<WarpState*>(encodeSmem)[warp];
+	SearchState& ss = reinterpret_cast<SearchState*>(encodeSmem + kWarpsPerCta * sizeof(WarpState))[warp];
+	const int n = *count;
+	const int heavy = n < nSplit ? n : nSplit;
+	for (;;)
+	{
+		int t = 0;
+		if (lane == 0)
+			t = atomicAdd(head, 1);
+		t = __shfl_sync(kFull, t, 0);
+		if (t >= heavy * NT)
+		{
+			const int i = heavy + (t - heavy * NT);
+			if (i >= n)
+				break;
+			const int k = list[i];
+			TexDesc d;
+			BlockRef b;
+			QueuedBlock(job, k, d, b);
+			const Params P = d.P;
+			if constexpr (kD == kAnyDenoise)
+			{
+				if (d.denoise)
+					PassStage<1, S>(st, ss, b, T1, P, sg.rec[k], sg.next[k], sg.start[k], lane);
+				else
+					PassStage<0, S>(st, ss, b, T0, P, sg.rec[k], sg.next[k], sg.start[k], lane);
+			}
+			else
+				PassStage<kD, S>(st, ss, b, kD ? T1 : T0, P, sg.rec[k], sg.next[k], sg.start[k], lane);
+			continue;
+		}
+		const int i = t / NT, p = t % NT;
+		const int k = list[i];
+		if (p < sg.start[k])
+			continue;
+		TexDesc d;
+		BlockRef b;
+		QueuedBlock(job, k, d, b);
+		const Params P = d.P;
+		if (P.pca && SplitMode(S) != 4 && SplitMode(S) != 5)
+		{
+			/* OPTION_PCA orders the partitions by their bounds first: the
+			   pass runs whole, in one warp */
+			if (p == 0 && lane == 0)
+				sg.firstImp[k] = kSplitSerial;
+			__syncwarp();
+			continue;
+		}
+		if constexpr (kD == kAnyDenoise)
+		{
+			if (d.denoise)
+				SplitTask<1, S>(st, ss, b, T1, P, sg, impCount, k, p, lane);
+			else
+				SplitTask<0, S>(st, ss, b, T0, P, sg, impCount, k, p, lane);
+		}
+		else
+			SplitTask<kD, S>(st, ss, b, kD ? T1 : T0, P, sg, impCount, k, p, lane);
+	}
+}
+
+/* Before the first round of a split pass: every block starts at candidate 0
+   with no improvement. */
+static __global__ void __launch_bounds__(256) KSplitPrepare(Stages sg, const int* list, const int* count)
+{
+	const int n = *count;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const int k = list[i];
+		sg.start[k] = 0;
+		sg.firstImp[k] = kSplitNone;
+	}
+}
+
+/* The commit of a round of split pass S, one thread per split block: the
+   first improving candidate f becomes the block's best and ends the pass,
+   or the block goes on from f + 1 in the next round's list (after the last
+   round, in the one-warp remainder's list); a block without an improvement
+   has finished the pass and gets its next one (NextStep). */
+template<int S>
+__global__ void __launch_bounds__(256) KSplitCommit(Job job, Stages sg, const int* list, const int* count, int nSplit, int* nextList,
+	int* nextCount, int* restList, int* restCount, int lastRound)
+{
+	constexpr int MODE = SplitMode(S);
+	/* the blocks after the first nSplit ran their whole pass in one task */
+	const int n = *count < nSplit ? *count : nSplit;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+	{
+		const int k = list[i];
+		const int f = sg.firstImp[k];
+		BlockRecord& r = sg.rec[k];
+		if (f == kSplitSerial)
+		{
+			sg.start[k] = 0;
+			restList[atomicAdd(restCount, 1)] = k;
+			continue;
+		}
+		int from = -1;
+		if (f != kSplitNone)
+		{
+			const int p = f >> 24, slot = f & 0xFFFFFF;
+			if (slot >= sg.impCap)
+				from = p;   /* its result was not kept: search it again */
+			else
+			{
+				const SplitResult e = sg.imp[slot];
+				r.errTotal = e.error;
+				r.best[0] = e.best0;
+				if (MODE != 4 && MODE != 5)
+					r.best[1] = e.best1;
+				r.bestParam = e.param;
+				r.bestMode = MODE;
+				if (!e.end && p < SplitTasks(S) - 1)
+					from = p + 1;
+			}
+		}
+		if (from >= 0)
+		{
+			sg.start[k] = from;
+			sg.firstImp[k] = kSplitNone;
+			if (lastRound)
+				restList[atomicAdd(restCount, 1)] = k;
+			else
+				nextList[atomicAdd(nextCount, 1)] = k;
+			continue;
+		}
+		TexDesc d;
+		BlockRef b;
+		QueuedBlock(job, k, d, b);
+		CellRegs R;
+		R.errTotal = r.errTotal;
+		R.opaqueAlphaError = r.opaqueAlphaError;
+		R.denoiseStep = r.denoiseStep;
+		R.a1.opaque = r.opaque != 0;
+		sg.next[k] = NextStep(S, R, d.P);
 	}
 }
 
@@ -553,14 +844,21 @@ template<int kD>
 cudaError_t StagedEncodeOccupancy(int* ctasPerSm);
 
 /* Bytes of the per-position state of a staged encode of n positions
-   (records, next-pass words and the pass list; 256-byte aligned pieces),
-   after kStagedZeroed bytes of counts and queue heads that must be zero
-   before each launch. */
-constexpr size_t kStagedZeroed = 256;
+   (records, next-pass words, the pass list, the split passes' start
+   partitions, first improvements, round lists and kept results; 256-byte
+   aligned pieces), after kStagedZeroed bytes of counts and queue heads that
+   must be zero before each launch. */
+constexpr size_t kStagedZeroed = 1024;
+
+constexpr size_t SplitResultCap(int n)
+{
+	return size_t(n) + 256;
+}
 
 constexpr size_t StagedScratchBytes(int n)
 {
-	return kStagedZeroed + ((size_t(n) * sizeof(BlockRecord) + 255) & ~size_t(255)) + ((size_t(n) * 4 + 255) & ~size_t(255)) * 2;
+	return kStagedZeroed + ((size_t(n) * sizeof(BlockRecord) + 255) & ~size_t(255)) + ((size_t(n) * 4 + 255) & ~size_t(255)) * 7 +
+		SplitResultCap(n) * sizeof(SplitResult);
 }
 
 /* Splits a staged scratch (256-byte aligned, StagedScratchBytes(n) bytes). */
@@ -569,10 +867,19 @@ inline Stages SplitStaged(uint8_t* p, int n)
 	Stages s;
 	s.count = (int*)p;
 	s.counters = (int*)(p + 128);
+	s.split = (int*)(p + 256);
 	s.rec = (BlockRecord*)(p + kStagedZeroed);
 	uint8_t* q = p + kStagedZeroed + ((size_t(n) * sizeof(BlockRecord) + 255) & ~size_t(255));
+	const size_t ints = (size_t(n) * 4 + 255) & ~size_t(255);
 	s.next = (int*)q;
-	s.list = (int*)(q + ((size_t(n) * 4 + 255) & ~size_t(255)));
+	s.list = (int*)(q + ints);
+	s.start = (int*)(q + 2 * ints);
+	s.firstImp = (int*)(q + 3 * ints);
+	s.splitList[0] = (int*)(q + 4 * ints);
+	s.splitList[1] = (int*)(q + 5 * ints);
+	s.splitList[2] = (int*)(q + 6 * ints);
+	s.imp = (SplitResult*)(q + 7 * ints);
+	s.impCap = int(SplitResultCap(n));
 	return s;
 }
 

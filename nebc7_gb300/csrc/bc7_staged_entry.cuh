@@ -8,6 +8,32 @@
 
 namespace nebc7 {
 
+/* The rounds of split pass STAGE over the list KStageListByError gathered:
+   round r's tasks, then its commit, which fills the next round's list; after
+   the last round the blocks still searching run the rest of the pass in
+   one warp each (KEncodeStage from their start partitions). */
+template<int kD, int STAGE>
+cudaError_t LaunchSplitStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
+{
+	int* c = sg.split + SplitIndex(STAGE) * 16;   /* [round][list length, task head, kept results] */
+	const int small = job.total < 256 ? 1 : ((job.total + 255) / 256 < 1216 ? (job.total + 255) / 256 : 1216);
+	KSplitPrepare<<<small, 256, 0, stream>>>(sg, sg.list, sg.count + STAGE);
+	for (int r = 0; r < kSplitRounds; r++)
+	{
+		const int* list = r ? sg.splitList[r - 1] : sg.list;
+		const int* count = r ? c + 4 * r : sg.count + STAGE;
+		const int nSplit = kSplitMaxBlocks;
+		KEncodeSplit<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, list, count, c + 4 * r + 1,
+			c + 4 * r + 2, nSplit, T0, T1);
+		const bool last = r == kSplitRounds - 1;
+		KSplitCommit<STAGE><<<small, 256, 0, stream>>>(job, sg, list, count, nSplit, last ? nullptr : sg.splitList[r],
+			last ? nullptr : c + 4 * (r + 1), sg.splitList[2], c + 4 * kSplitRounds, int(last));
+	}
+	KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, sg.splitList[2],
+		c + 4 * kSplitRounds, c + 4 * kSplitRounds + 1, T0, T1);
+	return cudaGetLastError();
+}
+
 template<int kD, int STAGE>
 cudaError_t LaunchStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
 {
@@ -17,8 +43,15 @@ cudaError_t LaunchStage(int grid, cudaStream_t stream, const Job& job, const Sta
 		KStageListByError<<<1, 1024, 0, stream>>>(sg.next, sg.rec, job.total, STAGE, sg.list, sg.count + STAGE);
 	else if (STAGE != kStageDraft)
 		KStageList<<<1, 1024, 0, stream>>>(sg.next, job.total, STAGE, sg.list, sg.count + (STAGE < 0 ? 0 : STAGE));
-	KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, T0, T1);
-	return cudaGetLastError();
+	if constexpr (SplitIndex(STAGE) >= 0)
+		return LaunchSplitStage<kD, STAGE>(grid, stream, job, sg, T0, T1);
+	else
+	{
+		const bool all = STAGE == kStageDraft;
+		KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, all ? nullptr : sg.list,
+			all ? nullptr : sg.count + STAGE, sg.counters + (STAGE + 1), T0, T1);
+		return cudaGetLastError();
+	}
 }
 
 template<int kD>
@@ -46,7 +79,12 @@ cudaError_t LaunchStagedEncode(int grid, cudaStream_t stream, const Job& job, co
 template<int kD, int STAGE>
 cudaError_t PrepareStage()
 {
-	return cudaFuncSetAttribute(KEncodeStage<kD, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(EncodeSharedBytes<true>()));
+	const cudaError_t e = cudaFuncSetAttribute(KEncodeStage<kD, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		int(EncodeSharedBytes<true>()));
+	if constexpr (SplitIndex(STAGE) >= 0)
+		if (e == cudaSuccess)
+			return cudaFuncSetAttribute(KEncodeSplit<kD, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(EncodeSharedBytes<true>()));
+	return e;
 }
 
 template<int kD>
