@@ -38,8 +38,10 @@ template<int kD, int STAGE>
 cudaError_t LaunchStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
 {
 	/* the passes after the draft chain take their blocks largest error
-	   first; the draft chain and the pack keep the queue order */
-	if (STAGE >= kStepRefine && STAGE < kStepFinish)
+	   first; the draft chain and the pack keep the queue order, and so do
+	   the passes of a mixed launch, whose queue keeps each texture's blocks
+	   (of one kDenoise) together */
+	if (kD != kAnyDenoise && STAGE >= kStepRefine && STAGE < kStepFinish)
 		KStageListByError<<<1, 1024, 0, stream>>>(sg.next, sg.rec, job.total, STAGE, sg.list, sg.count + STAGE);
 	else if (STAGE != kStageDraft)
 		KStageList<<<1, 1024, 0, stream>>>(sg.next, job.total, STAGE, sg.list, sg.count + (STAGE < 0 ? 0 : STAGE));
