@@ -161,7 +161,9 @@ def issue_roofline(prof, kernel_ms, sm_mhz, n_sms):
     sources (None when the capture is of another build, or without a clock
     sample).  kernel_ms is the CUDA-event time of the encode call: KEncode
     plus, for the refining presets, the two block-order kernels in front of
-    it (KBlockBuckets, KBlockOrder; about 13 us of a 5.6 ms call)."""
+    it (KBlockBuckets, KBlockOrder; about 13 us of a 5.5 ms call); for a
+    staged encode every pass kernel, and the capture's instruction count is
+    the sum over the same launches."""
     prof = current_capture(prof)
     if not prof or not prof.get("warp_inst_per_launch") or not sm_mhz or not kernel_ms or kernel_ms <= 0:
         return None
@@ -481,10 +483,11 @@ def run_ours(args, rank, world, local):
         roofline.update({"kernel_ms": kernel_ms, "hbm": hbm, "issue_ncu": issue_ncu, "work": work,
                          "build_source_sha": source_sha(),
                          "note": "integer-issue and latency bound search. frac: executed warp instructions "
-                                 "(ncu, same CUDA sources) over the issue peak; work: the reference's algorithmic "
-                                 "int ops over the integer-lane peak; hbm: algorithmic input/output bytes, of "
-                                 "measured peak. kernel_ms covers the encode call (KBlockBuckets + KBlockOrder "
-                                 "+ KEncode for the refining presets, KEncode alone for draft)"})
+                                 "of the encode call (ncu, same CUDA sources) over the issue peak; work: the "
+                                 "reference's algorithmic int ops over the integer-lane peak; hbm: algorithmic "
+                                 "input/output bytes, of measured peak. kernel_ms covers the encode call: "
+                                 "KBlockBuckets + KBlockOrder + KEncode for the single-kernel presets, every "
+                                 "pass kernel of the staged encode for precise, /slow and /data"})
         cpu = {"value": cpu_value, "unit": "Mpx/s", "cores": cores, "kind": "port", "sample": sample,
                "reference_simd_equiv": simd_equivalent(args.workload, cpu_value)}
         line = {

@@ -41,13 +41,19 @@ def test_issue_roofline_needs_capture_clock_and_time(prof, ms, mhz):
 
 
 def test_committed_captures_have_the_fields_the_bench_reads():
+    """Every workload's capture has its per-encode instructions and DRAM bytes
+    and names its summary; the single-kernel workload's full-set capture also
+    has the issue and pipe utilisation.  The captures are of one build."""
     profs = json.loads((ROOT / "profiles" / "kencode_ncu.json").read_text())
     assert "photo1024_default" in profs
     for prof in profs.values():
-        for key in ("dram_bytes_per_launch", "sm_issue_active_pct_elapsed", "pipe_alu_pct_active",
-                    "pipe_fma_pct_active", "warp_inst_per_launch", "summary", "source_sha"):
+        for key in ("dram_bytes_per_launch", "warp_inst_per_launch", "summary", "source_sha"):
             assert key in prof
+        assert prof["warp_inst_per_launch"] > 0
         assert (ROOT / "profiles" / prof["summary"]).exists()
+    for key in ("sm_issue_active_pct_elapsed", "pipe_alu_pct_active", "pipe_fma_pct_active"):
+        assert key in profs["photo1024_default"]
+    assert len({p["source_sha"] for p in profs.values()}) == 1
 
 
 def test_simd_equivalent_scales_the_port_by_the_calibration():
