@@ -158,8 +158,9 @@ int nebc7_set_pca(int on);
 /* How many kernels one nebc7_encode_device call with these settings
    launches (the block order, then the encode: one persistent kernel, or
    for the presets whose time goes to the full searches the staged form of
-   a kernel per pass and a list kernel before each), not counting the sums'
-   reduction; a negative error code for invalid settings. */
+   a kernel per pass and a list kernel before each, the split passes with a
+   task and a commit kernel per round), not counting the sums' reduction;
+   a negative error code for invalid settings. */
 int nebc7_encode_launches(const nebc7_settings* settings);
 
 /* Builds the level tables of `denoise` on the current device ahead of use. */

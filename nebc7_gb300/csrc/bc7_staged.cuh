@@ -35,7 +35,7 @@
  * The round's commit applies f and ends the pass, or the block continues
  * in the next round from candidate f + 1 with the new error.  Improvements
  * are rare, so most blocks finish in the first round; blocks still
- * searching after kSplitRounds rounds finish their pass in one warp each.
+ * searching after SplitRounds(S) rounds finish their pass in one warp each.
  */
 #pragma once
 
@@ -91,7 +91,7 @@ struct __align__(16) SplitResult
 };
 
 /* The split passes and their rounds. */
-constexpr int kSplitRounds = 3;
+constexpr int kSplitMaxRounds = 8;
 constexpr int kSplitMaxBlocks = 1 << 24;    /* blocks of a round split into partition tasks (the task count stays an int) */
 constexpr int kSplitSerial = -1;            /* firstImp: the block's pass runs whole (OPTION_PCA) */
 constexpr int kSplitNone = 0x7FFFFFFF;      /* firstImp: no improvement yet */
@@ -112,6 +112,29 @@ __host__ __device__ constexpr int SplitMode(int S)
 	return S == kStepFull2Mode1 ? 1 : (S == kStepFull2Mode3 ? 3 : (S == kStepRot5 ? 5 : (S == kStepRot4 ? 4 : 7)));
 }
 
+/* Rounds of split pass S: one per candidate for the rotation searches,
+   whose choices often improve one after another; three for the partition
+   searches, where a block rarely improves more than twice. */
+__host__ __device__ constexpr int SplitRounds(int S)
+{
+	return S == kStepRot4 || S == kStepRot5 ? SplitTasks(S) : 3;
+}
+
+/* Kernel launches of one staged encode: the draft kernel, then per pass its
+   list and its kernel, or for a split pass its list, the preparation, a
+   task and a commit kernel per round and the one-warp rest. */
+__host__ __device__ constexpr int StagedLaunches()
+{
+	int n = 1;
+	for (int S = 0; S < kNumStages; S++)
+		n += SplitIndex(S) >= 0 ? 3 + 2 * SplitRounds(S) : 2;
+	return n;
+}
+
+/* Ints of the zeroed split counters per split pass: [round][list length,
+   task head, kept results, unused], the last row for the one-warp rest. */
+constexpr int kSplitCounterInts = 4 * (kSplitMaxRounds + 1);
+
 /* Per-launch state of a staged encode (one entry per queue position). */
 struct Stages
 {
@@ -123,8 +146,8 @@ struct Stages
 	/* split passes */
 	int* start;       /* per position: the first candidate of the block's next round */
 	int* firstImp;    /* per position: (candidate << 24) | result slot of the round's first improvement */
-	int* splitList[3];   /* the lists of rounds 1 and 2 and of the one-warp remainder */
-	int* split;       /* [5 split passes][4][4] list lengths, task heads, result counts; zero before the draft kernel */
+	int* splitList[3];   /* the lists of the later rounds (alternately) and of the one-warp remainder */
+	int* split;       /* [5 split passes][kSplitCounterInts] list lengths, task heads, result counts; zero before the draft kernel */
 	SplitResult* imp;
 	int impCap;
 };
@@ -848,7 +871,7 @@ cudaError_t StagedEncodeOccupancy(int* ctasPerSm);
    partitions, first improvements, round lists and kept results; 256-byte
    aligned pieces), after kStagedZeroed bytes of counts and queue heads that
    must be zero before each launch. */
-constexpr size_t kStagedZeroed = 1024;
+constexpr size_t kStagedZeroed = 1280;
 
 constexpr size_t SplitResultCap(int n)
 {

@@ -15,22 +15,26 @@ namespace nebc7 {
 template<int kD, int STAGE>
 cudaError_t LaunchSplitStage(int grid, cudaStream_t stream, const Job& job, const Stages& sg, const LevelTables& T0, const LevelTables& T1)
 {
-	int* c = sg.split + SplitIndex(STAGE) * 16;   /* [round][list length, task head, kept results] */
+	constexpr int kRounds = SplitRounds(STAGE);
+	static_assert(kRounds <= kSplitMaxRounds, "the split counters hold kSplitMaxRounds rounds");
+	int* c = sg.split + SplitIndex(STAGE) * kSplitCounterInts;   /* [round][list length, task head, kept results] */
 	const int small = job.total < 256 ? 1 : ((job.total + 255) / 256 < 1216 ? (job.total + 255) / 256 : 1216);
 	KSplitPrepare<<<small, 256, 0, stream>>>(sg, sg.list, sg.count + STAGE);
-	for (int r = 0; r < kSplitRounds; r++)
+	/* round r > 0 reads the list round r - 1's commit wrote: the two round
+	   lists alternate */
+	for (int r = 0; r < kRounds; r++)
 	{
-		const int* list = r ? sg.splitList[r - 1] : sg.list;
+		const int* list = r ? sg.splitList[(r - 1) & 1] : sg.list;
 		const int* count = r ? c + 4 * r : sg.count + STAGE;
 		const int nSplit = kSplitMaxBlocks;
 		KEncodeSplit<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, list, count, c + 4 * r + 1,
 			c + 4 * r + 2, nSplit, T0, T1);
-		const bool last = r == kSplitRounds - 1;
-		KSplitCommit<STAGE><<<small, 256, 0, stream>>>(job, sg, list, count, nSplit, last ? nullptr : sg.splitList[r],
-			last ? nullptr : c + 4 * (r + 1), sg.splitList[2], c + 4 * kSplitRounds, int(last));
+		const bool last = r == kRounds - 1;
+		KSplitCommit<STAGE><<<small, 256, 0, stream>>>(job, sg, list, count, nSplit, last ? nullptr : sg.splitList[r & 1],
+			last ? nullptr : c + 4 * (r + 1), sg.splitList[2], c + 4 * kSplitMaxRounds, int(last));
 	}
 	KEncodeStage<kD, STAGE><<<grid, kWarpsPerCta * 32, EncodeSharedBytes<true>(), stream>>>(job, sg, sg.splitList[2],
-		c + 4 * kSplitRounds, c + 4 * kSplitRounds + 1, T0, T1);
+		c + 4 * kSplitMaxRounds, c + 4 * kSplitMaxRounds + 1, T0, T1);
 	return cudaGetLastError();
 }
 

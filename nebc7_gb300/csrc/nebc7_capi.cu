@@ -1688,7 +1688,7 @@ int nebc7_encode_launches(const nebc7_settings* settings)
 	if (int e = ValidateSettings(settings))
 		return -SetError(e);
 	const int order = OrdersBlocks(*settings) ? 2 : 0;
-	return order + (SlotStaged(VariantSlot(*settings)) ? 1 + 2 * kNumStages : 1);
+	return order + (SlotStaged(VariantSlot(*settings)) ? StagedLaunches() : 1);
 }
 
 int nebc7_init_device(int denoise)
