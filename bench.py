@@ -319,6 +319,18 @@ def run_reference_serve(args, world):
         "e2e": {"value": value, "unit": "Mpx/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def max_over_ranks(values, world, device=None):
+    """Each value's maximum over the ranks (the slowest replica's time), the
+    values unchanged on one rank.  The replicas' only collective."""
+    if world <= 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.cpu()]
+
+
 def run_reference(args, rank, world):
     """CPU baseline arm: the oracle port on all host cores, rank 0 only."""
     if rank != 0:
@@ -409,11 +421,9 @@ def run_ours(args, rank, world, local):
     wall = time.time() - wall0
     step_ms = sum(a.elapsed_time(b) for a, b in zip(starts, ends)) / args.steps
     kernel_ms = sum(a.elapsed_time(b) for a, b in zip(mids, ends)) / args.steps
+    step_ms, kernel_ms = max_over_ranks([step_ms, kernel_ms], world, dev)
     if world > 1:
         import torch.distributed as dist
-        t = torch.tensor([step_ms, kernel_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms, kernel_ms = float(t[0]), float(t[1])
         dist.barrier()
 
     px = pw * ph
@@ -535,6 +545,9 @@ def run_batch(args, rank, world, local):
 
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
     nebc7_gb300.build()
     lib = nebc7_gb300.load()
     for d in (0, 1):
@@ -578,6 +591,9 @@ def run_batch(args, rank, world, local):
     torch.cuda.synchronize()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
     with NvmlSampler(dev) as clocks:
         for i in range(args.steps):
             starts[i].record(stream)
@@ -585,6 +601,7 @@ def run_batch(args, rank, world, local):
             ends[i].record(stream)
         torch.cuda.synchronize()
     step_ms = sum(a.elapsed_time(c) for a, c in zip(starts, ends)) / args.steps
+    step_ms, = max_over_ranks([step_ms], world, dev)
     exact = all(torch.equal(t["dst"], o) for t, o in zip(texs, plain_out))
 
     # end to end: pinned host inputs in, blocks out, every step
@@ -648,6 +665,9 @@ def run_batch(args, rank, world, local):
             "clocks": clocks.summary(),
         }
         print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
 
 
 SERVE_PRESETS = (("default", (1, 9, 1, 1, 0, 0), 50), ("draft", (1, 9, 1, 0, 0, 0), 30),
