@@ -315,7 +315,8 @@ typedef struct nebc7_server_counters
    cheapest requests dealt first; each request of a light batch returns
    (its blocks copied back) as soon as its own blocks are done, while the
    rest of the launch still runs.  Besides the arena, every stream holds the
-   staged form's records: 104 bytes per block for up to min(4194304,
+   staged form's per-block state (its record, pass lists, split-pass rounds
+   and kept results): 156 bytes per block for up to min(4194304,
    hbm_budget / 104) blocks. */
 int nebc7_server_create(const nebc7_server_config* cfg, nebc7_server** out);
 
