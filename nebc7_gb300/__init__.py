@@ -11,6 +11,6 @@ from . import synth  # noqa: F401
 from ._native import build, load, NativeError  # noqa: F401
 from .api import (  # noqa: F401
     Bc7Core, Preset, DEFAULT, PRECISE, EncodeStats, EncodedImage,
-    encode_image, encode_device, set_pca, pad_texture, outline_mask, padded_size, parse_flags, Batch, BatchTexture, Server,
+    encode_image, encode_device, set_pca, pad_texture, outline_mask, padded_size, parse_flags, Batch, BatchTexture, PlanStore, plan_key, Server,
     ktx_header, write_ktx, read_ktx,
 )

@@ -262,6 +262,44 @@ class BatchTexture:
     settings: Settings
 
 
+def plan_key(textures: list[BatchTexture], device: str) -> str:
+    """The (preset mix, GPU) a tuned batch plan is kept for: the device name
+    and, per preset, its blocks rounded down to a power of two, so that
+    batches of the same mix and about the same size share a plan."""
+    mix: dict[tuple, int] = {}
+    for t in textures:
+        s = t.settings
+        k = (s.denoise, s.denoiseStep, s.doDraft, s.doNormal, s.doSlow, s.linearData)
+        mix[k] = mix.get(k, 0) + (t.width // 4) * (t.height // 4)
+    parts = [f"{'-'.join(map(str, k))}:{1 << max(0, v.bit_length() - 1)}" for k, v in sorted(mix.items())]
+    return device + "|" + ",".join(parts)
+
+
+class PlanStore:
+    """Tuned batch plans in a JSON file, one per plan_key, so that a batch of
+    a known mix on a known GPU starts from its plan instead of tuning."""
+
+    def __init__(self, path):
+        import pathlib
+        self.path = pathlib.Path(path)
+
+    def _read(self) -> dict:
+        import json
+        return json.loads(self.path.read_text()) if self.path.exists() else {}
+
+    def get(self, key: str) -> dict | None:
+        return self._read().get(key)
+
+    def put(self, key: str, plan: dict) -> None:
+        import json
+        import os
+        plans = self._read()
+        plans[key] = {"schedule": plan["schedule"], "staged": bool(plan["staged"]), "ctas_per_sm": int(plan["ctas_per_sm"])}
+        tmp = self.path.with_suffix(self.path.suffix + ".tmp")
+        tmp.write_text(json.dumps(plans, indent=1, sort_keys=True))
+        os.replace(tmp, self.path)
+
+
 class Batch:
     """Many textures of any sizes and presets encoded by one plan: a
     persistent launch over a global block queue (or one per preset group on
@@ -271,6 +309,7 @@ class Batch:
     MIXED, GROUPED = 0, 1
 
     def __init__(self, textures: list[BatchTexture], from_scratch: bool = False):
+        self._textures = list(textures)
         self._lib = _native.load()
         arr = (_native.Texture * len(textures))()
         for i, t in enumerate(textures):
@@ -288,7 +327,10 @@ class Batch:
                                            ctypes.byref(self._h)), "batch_create")
 
     def tune(self, trials: int = 2) -> tuple[float, float]:
-        """Times both schedules and keeps the faster; returns their best ms."""
+        """Searches the plan's knobs (schedule, staged form, CTAs per SM),
+        timing each candidate `trials` times as a CUDA graph, and keeps the
+        fastest (trials() lists them); returns the best ms of the mixed and
+        the grouped schedule."""
         ms = (ctypes.c_float * 2)()
         check(self._lib.nebc7_batch_tune(self._h, trials, ctypes.cast(ms, ctypes.c_void_p)), "batch_tune")
         return float(ms[0]), float(ms[1])
@@ -304,6 +346,20 @@ class Batch:
 
     def set_plan(self, schedule: int, staged: bool, ctas_per_sm: int = 0) -> None:
         check(self._lib.nebc7_batch_set_plan(self._h, schedule, int(staged), ctas_per_sm), "batch_set_plan")
+
+    def tune_cached(self, store: PlanStore, device: str, trials: int = 2) -> tuple[dict, bool]:
+        """The plan kept in `store` for this batch's mix on `device` if there
+        is one, else tune() and keep its choice; returns the plan and whether
+        it was tuned now."""
+        key = plan_key(self._textures, device)
+        plan = store.get(key)
+        if plan is not None:
+            self.set_plan(("mixed", "grouped").index(plan["schedule"]), plan["staged"], plan["ctas_per_sm"])
+            return self.plan(), False
+        self.tune(trials)
+        plan = self.plan()
+        store.put(key, plan)
+        return plan, True
 
     def trials(self) -> list[dict]:
         """The plans the last tune timed, in order, with their best ms."""
