@@ -42,7 +42,7 @@ enum
 	NEBC7_EINVAL = 1,        /* bad argument (sizes, alignment, preset) */
 	NEBC7_ECUDA = 2,         /* a CUDA call failed */
 	NEBC7_ENOMEM = 3,        /* device memory could not be allocated */
-	NEBC7_EUNSUPPORTED = 4,  /* requested pass not available in this build */
+	NEBC7_EUNSUPPORTED = 4,  /* requested pass not compiled into the library */
 	NEBC7_ELIMIT = 5,        /* a device-side iteration limit was reached */
 	NEBC7_ETOOBIG = 6        /* request exceeds a fixed capacity */
 };

@@ -214,7 +214,7 @@ class NativeError(RuntimeError):
         1: "invalid argument",
         2: "CUDA call failed",
         3: "device memory allocation failed",
-        4: "pass not available in this build",
+        4: "pass not compiled into the library",
         5: "device iteration limit reached",
         6: "request exceeds a fixed capacity",
     }

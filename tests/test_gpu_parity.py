@@ -44,7 +44,7 @@ def needs(native, st):
     (NEBC7_EUNSUPPORTED) fails the case instead of skipping it."""
     z = np.zeros((1, 64), np.uint8)
     rc, _, _ = gpu_blocks(native, z, np.full((1, 64), 255, np.uint8), np.zeros((1, 16), np.uint8), st)
-    assert rc != 4, "this library build lacks the passes of these settings"
+    assert rc != 4, "the library lacks the passes of these settings"
     assert rc == 0
 
 
